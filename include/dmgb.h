@@ -1,0 +1,298 @@
+/*
+ * dmgb.h - C ABI of the GB300 DistMesh engine (libdmgb.so).
+ *
+ * Every entry point returns an int status (DM_OK == 0).  Pointers marked
+ * "device" are CUDA device pointers; "stream" is a cudaStream_t passed as
+ * void*.  The library never allocates device memory on the paths declared
+ * here: callers pass workspaces sized by the matching *_workspace_size call.
+ * Kernels report data-dependent failures through a device counters block
+ * (int64_t[DM_NCOUNTERS]) that the caller reads when it synchronises.
+ *
+ * Point layout: 2D points are float[n][2]; 3D points are float[n][4] (x, y,
+ * z, unused) so that one point is one aligned 16-byte load.
+ *
+ * Each declaration names the reference interface it replaces
+ * (path:line inside the SeismicMesh project).
+ */
+#ifndef DMGB_H
+#define DMGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define DM_OK 0
+#define DM_ERR_ARG 1           /* bad argument (shape, size, pointer)      */
+#define DM_ERR_CUDA 2          /* a CUDA runtime call failed               */
+#define DM_ERR_CAPACITY 3      /* an output buffer was too small           */
+#define DM_ERR_NOT_CONVERGED 4 /* bounded iteration hit its limit          */
+#define DM_ERR_DEGENERATE 5    /* degenerate input (duplicates, flat set)  */
+#define DM_ERR_WORKSPACE 6     /* workspace smaller than required          */
+
+/* ---- device counters block: indices into int64_t[DM_NCOUNTERS] --------- */
+#define DM_CNT_CELLS 0       /* cells written by dm_delaunay               */
+#define DM_CNT_ESCALATED 1   /* vertices resolved by the exhaustive search */
+#define DM_CNT_FLAGS 2       /* OR of DM_FLAG_* bits                       */
+#define DM_CNT_KEPT 3        /* cells kept by dm_filter_cells              */
+#define DM_CNT_EDGES 4       /* unique edges counted by dm_adjacency       */
+#define DM_CNT_BAD 5         /* cells flagged by dm_dihedral_flags         */
+#define DM_CNT_DUPS 6        /* duplicate points found by dm_delaunay      */
+#define DM_CNT_AUX 7
+#define DM_NCOUNTERS 16
+
+#define DM_FLAG_CELL_OVERFLOW 1   /* cells capacity exceeded               */
+#define DM_FLAG_STAR_OVERFLOW 2   /* a vertex star exceeded its capacity   */
+#define DM_FLAG_SEED_FAILED 4     /* no Delaunay seed found for a vertex   */
+#define DM_FLAG_DUPLICATES 8      /* exactly coincident input points       */
+#define DM_FLAG_EXACT_OVERFLOW 16 /* exact arithmetic capacity exceeded    */
+#define DM_FLAG_ADJ_OVERFLOW 32   /* adjacency row capacity exceeded       */
+#define DM_FLAG_DIVERGED 64       /* max movement >= 1000 h0               */
+#define DM_FLAG_NONFINITE 128     /* NaN/Inf in positions                  */
+
+/* ---- signed distance programs ------------------------------------------
+ * A domain is a postfix program of primitives and set operations, see
+ * seismicmesh_gb300/geometry/signed_distance_functions.py for the encoder.
+ * ops/params live in device memory. */
+typedef struct dm_sdf_program {
+  const int32_t *ops;   /* device: n_ops records of DM_SDF_OPREC ints      */
+  const float *params;  /* device: parameter pool                          */
+  int32_t n_ops;
+  int32_t dim;
+} dm_sdf_program;
+
+/* ---- sizing functions ------------------------------------------------- */
+#define DM_SIZING_CONST 0 /* h(x) = h                                      */
+#define DM_SIZING_GRID 1  /* linear interpolation on a regular grid,        */
+                          /* extrapolating (RegularGridInterpolator,        */
+                          /* bounds_error=False, fill_value=None)           */
+#define DM_SIZING_SLOTS 2 /* per adjacency slot values supplied by caller   */
+typedef struct dm_sizing {
+  int32_t kind;
+  int32_t dim;
+  float h;              /* DM_SIZING_CONST                                  */
+  const float *grid;    /* device, C order (n0, n1[, n2])                   */
+  int32_t n[3];
+  float lo[3], hi[3];   /* axis k spans linspace(lo[k], hi[k], n[k])        */
+  const float *slot_h;  /* device, [n_points * adj_cap] for DM_SIZING_SLOTS */
+} dm_sizing;
+
+/* ---- library ----------------------------------------------------------- */
+int dm_version(void);
+/* message of the last failing call on this host thread */
+const char *dm_last_error(void);
+/* number of entry points listed in this header (for loader self-checks) */
+int dm_abi_count(void);
+
+/* ---- exact predicates on the host (FP32 inputs) -------------------------
+ * Replace the filtered Epick predicates CGAL uses inside the triangulations
+ * (generation/cpp/delaunay_class3.cpp:116-129).  Return -1/0/+1; the _sos
+ * variants apply the lexicographic symbolic perturbation and return 0 only
+ * for five coplanar (four collinear) points. */
+int dm_orient2(const float *a, const float *b, const float *c);
+int dm_orient3(const float *a, const float *b, const float *c, const float *d);
+int dm_incircle_sos(const float *a, const float *b, const float *c,
+                    const float *d);
+int dm_insphere_sos(const float *a, const float *b, const float *c,
+                    const float *d, const float *e);
+
+/* ---- Delaunay triangulation -------------------------------------------
+ * Replaces DelaunayTriangulation{,3}.insert + get_finite_cells
+ * (generation/cpp/delaunay_class.cpp:108-121,232-265;
+ *  generation/cpp/delaunay_class3.cpp:116-129,276-310) as called from
+ * generation/mesh_generator.py:465-469.  Writes every finite cell once,
+ * positively oriented, as int32[cap_cells][dim+1] (device).  Vertex indices
+ * are the input indices (no renumbering).  counters (device, zeroed by the
+ * call) receives DM_CNT_CELLS / _ESCALATED / _FLAGS / _DUPS. */
+int dm_delaunay_workspace_size(int32_t dim, int64_t n, size_t *bytes);
+int dm_delaunay(int32_t dim, const float *points, int64_t n, int32_t *cells,
+                int64_t cap_cells, int64_t *counters, void *workspace,
+                size_t workspace_bytes, void *stream);
+
+/* ---- cell filter ---------------------------------------------------------
+ * Replaces _remove_triangles_outside (generation/mesh_generator.py:734-738):
+ * keeps cells whose centroid c has sdf(c) < -geps.  n_cells is read from
+ * counters[DM_CNT_CELLS] (device); the kept count goes to
+ * counters[DM_CNT_KEPT].  The order of kept cells is unspecified (so is the
+ * Delaunay output order; every consumer is order-free). */
+int dm_filter_cells_workspace_size(int64_t cap_cells, size_t *bytes);
+int dm_filter_cells(int32_t dim, const float *points, const int32_t *cells,
+                    int64_t cap_cells, const dm_sdf_program *sdf, float geps,
+                    int32_t *cells_out, int64_t *counters, void *workspace,
+                    size_t workspace_bytes, void *stream);
+/* centroids of the first counters[DM_CNT_CELLS] cells, float[cap][dim] */
+int dm_cell_centroids(int32_t dim, const float *points, const int32_t *cells,
+                      int64_t cap_cells, const int64_t *counters,
+                      float *centroids, void *stream);
+
+/* ---- bars (unique edges) ------------------------------------------------
+ * Replaces _get_edges + _fast_geometry.unique_edges
+ * (generation/mesh_generator.py:680-688, geometry/cpp/fast_geometry.cpp:30-77)
+ * in the adjacency form the force kernels consume: row v of adj
+ * (int32[n][adj_cap], device) lists the neighbours of v in increasing order,
+ * deg[v] their count.  Cells are read from `cells` with count
+ * counters[count_index].  counters[DM_CNT_EDGES] receives the number of
+ * unique edges. */
+int dm_adjacency(int32_t dim, int64_t n, const int32_t *cells,
+                 int64_t cap_cells, int32_t count_index, int32_t *adj,
+                 int32_t adj_cap, int32_t *deg, int64_t *counters,
+                 void *stream);
+/* Drop-in unique_edges: edges int32[m][2] -> sorted unique (min,max) pairs.
+ * Needs the vertex count bound n (max index + 1). */
+int dm_unique_edges_workspace_size(int64_t n, int64_t m, size_t *bytes);
+int dm_unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
+                    int64_t *n_out_host, void *workspace,
+                    size_t workspace_bytes, void *stream);
+
+/* ---- bar forces and point update ---------------------------------------
+ * Replaces _compute_forces + dense scatter + position update + Newton
+ * projection (generation/mesh_generator.py:497-506,691-712,762-784,
+ * generation/utils.py:48-68).  Two passes over the adjacency:
+ *   dm_bar_sums      per-block partial sums of L^dim and h^dim over
+ *                    unique bars (v < w), written to partials[2*nblk];
+ *   dm_update_points F = sum_w max(L0 - L, 0) / L * (p_v - p_w), with
+ *                    L0 = h * L0mult * (sum L^d / sum h^d)^(1/d); points
+ *                    with index < nfix keep F = 0;
+ *                    p' = p + dt F, then one Newton step back onto the
+ *                    zero level set of every program in `levels`
+ *                    (level 0: points with d > 0; level k > 0: points with
+ *                    0 < d < hmin / 1.5).  Writes points_out, per-block
+ *                    maxima of |F| into maxf[0..nblk) and their maximum
+ *                    into maxf[nblk].
+ * dm_bar_blocks gives nblk for n points; partials holds 2*nblk + 3 doubles
+ * (partials[2*nblk] = the L0 scale, then sum L^d and sum h^d). */
+int dm_bar_blocks(int64_t n, int32_t *nblk);
+int dm_bar_sums(int32_t dim, const float *points, int64_t n,
+                const int32_t *adj, int32_t adj_cap, const int32_t *deg,
+                const dm_sizing *sizing, double *partials, void *stream);
+int dm_update_points(int32_t dim, const float *points, float *points_out,
+                     int64_t n, const int32_t *adj, int32_t adj_cap,
+                     const int32_t *deg, const dm_sizing *sizing,
+                     const double *partials, float L0mult, float delta_t,
+                     int64_t nfix, const dm_sdf_program *levels,
+                     int32_t n_levels, float hmin, float deps, float *maxf,
+                     void *stream);
+/* bar midpoints per adjacency slot (float[n][adj_cap][dim]) for sizing
+ * functions that are host callables */
+int dm_slot_midpoints(int32_t dim, const float *points, int64_t n,
+                      const int32_t *adj, int32_t adj_cap, const int32_t *deg,
+                      float *mid, void *stream);
+
+/* ---- signed distance and sizing evaluation ------------------------------
+ * Replace geometry.*.eval (geometry/signed_distance_functions.py:89-101,
+ * 307-623, geometry/cpp/fast_geometry.cpp:104-214) and SizeFunction.eval
+ * (sizing/size_function.py:11-12, sizing/mesh_size_function.py:391-408).
+ * x is float[n][x_stride]; grad (optional, may be NULL) float[n][dim]. */
+int dm_sdf_eval(const dm_sdf_program *sdf, const float *x, int64_t n,
+                int32_t x_stride, float *d, float *grad, void *stream);
+int dm_sizing_eval(const dm_sizing *sizing, const float *x, int64_t n,
+                   int32_t x_stride, float *h, void *stream);
+
+/* ---- level-set improvement ----------------------------------------------
+ * Replaces _improve_level_set_newton (generation/mesh_generator.py:741-759):
+ * 5 damped Newton steps on the listed vertices. */
+int dm_improve_level_set(int32_t dim, float *points, const int32_t *ids,
+                         int64_t n_ids, const dm_sdf_program *sdf, float deps,
+                         void *stream);
+
+/* ---- sliver kernels -------------------------------------------------------
+ * Replace calc_dihedral_angles / calc_circumsphere_grad
+ * (geometry/cpp/fast_geometry.cpp:351-418, 580-666) and the sliver
+ * selection of sliver_removal (generation/mesh_generator.py:222-274). */
+int dm_dihedral_angles(const float *points, const int32_t *cells, int64_t nc,
+                       double *angles, void *stream);
+int dm_circumsphere_grad(const double *p0, const double *p1, const double *p2,
+                         const double *p3, int64_t m, double *grad,
+                         void *stream);
+/* flags[c] = 1 when a dihedral angle of cell c is outside [min, max]
+ * (radians); counters[DM_CNT_BAD] receives the count. */
+int dm_dihedral_flags(const float *points, const int32_t *cells,
+                      int64_t cap_cells, int32_t count_index, float min_angle,
+                      float max_angle, int32_t *flags, int64_t *counters,
+                      void *stream);
+/* perturb vertex 0 of each flagged cell by step*h0*normalize(grad R^2),
+ * all perturbations computed from the pre-update positions; when a vertex is
+ * vertex 0 of several flagged cells the highest cell index wins (numpy's
+ * buffered fancy-index += keeps the last duplicate). */
+int dm_sliver_workspace_size(int64_t n_points, size_t *bytes);
+int dm_sliver_perturb(float *points, int64_t n_points, const int32_t *cells,
+                      int64_t cap_cells, int32_t count_index,
+                      const int32_t *flags, float step_h0, void *workspace,
+                      size_t workspace_bytes, int64_t *counters, void *stream);
+
+/* ---- gradient limiting -----------------------------------------------------
+ * Replaces _FastHJ.limgrad (sizing/cpp/FastHJ.cpp:63-157): limits
+ * |grad f| <= dfdx on a column-major (dims[0], dims[1], dims[2]) grid with
+ * 6-neighbour spacing elen, to the relaxation's fixed point. f is updated in
+ * place (device, float64). */
+int dm_limgrad(const int32_t *dims_host, double elen, double dfdx,
+               int32_t imax, double *f, void *stream);
+
+/* ---- sizing grids ----------------------------------------------------------
+ * Elementwise part of get_sizing_function_from_segy
+ * (sizing/mesh_size_function.py:146-221): vp (device, float64[n], updated
+ * in place) *= scale; when some vp < 1e-3 lies outside the first row_len
+ * entries they become vp_water; cell_size = clamp(min(vp/(freq*wl) if wl>0,
+ * gradient_term if grad>0), hmin, hmax), then the Courant bound when
+ * dt, cr_max and space_order are non-zero.  gradient_term may be NULL when
+ * grad == 0.  workspace: >= 4 bytes of device memory. */
+int dm_size_from_velocity(double *vp, int64_t n, int64_t row_len,
+                          const double *gradient_term, double scale,
+                          double vp_water, double wl, double freq, double grad,
+                          double hmin, double hmax, double dt, double cr_max,
+                          double space_order, int32_t dim, double *cell_size,
+                          int32_t *replaced_host, void *workspace,
+                          size_t workspace_bytes, void *stream);
+/* numpy.pad of a C-order float64 grid (_pad_it, mesh_size_function.py:
+ * 575-587): mode 0 edge, 1 constant, 2 linear_ramp (to cval). */
+int dm_pad_grid(const double *src, const int32_t *n_host,
+                const int32_t *pre_host, const int32_t *post_host, int32_t dim,
+                int32_t mode, double cval, double *dst, void *stream);
+
+/* ---- termination topology ------------------------------------------------
+ * dm_boundary replaces get_boundary_edges / get_boundary_facets /
+ * get_boundary_vertices (geometry/utils.py:310-326,364-382,421-437): facets
+ * (edges in 2D, triangles in 3D) that occur in exactly one of the cells
+ * counters[count_index] of `cells`; vertex_flags[v] = 1 for their vertices;
+ * faces_out (optional, int32[faces_cap][dim]) receives them, their count in
+ * counters[DM_CNT_AUX]. */
+int dm_boundary_workspace_size(int32_t dim, int64_t n, int64_t cap_cells,
+                               size_t *bytes);
+int dm_boundary(int32_t dim, int64_t n, const int32_t *cells, int64_t cap_cells,
+                int32_t count_index, int32_t *vertex_flags, int32_t *faces_out,
+                int64_t faces_cap, int64_t *counters, void *workspace,
+                size_t workspace_bytes, void *stream);
+/* fix_mesh(delete_unused=True) for a duplicate-free, positively oriented
+ * cell set (geometry/utils.py:204-249): removes vertices no cell uses,
+ * renumbers cells in place (order kept), gathers points_out; synchronises
+ * and returns the new vertex count in *n_out_host. */
+int dm_compact_workspace_size(int64_t n, size_t *bytes);
+int dm_compact_vertices(int32_t dim, const float *points, float *points_out,
+                        int64_t n, int32_t *cells, int64_t cap_cells,
+                        int32_t count_index, int64_t *counters,
+                        int64_t *n_out_host, void *workspace,
+                        size_t workspace_bytes, void *stream);
+/* simp_vol / simp_qual (geometry/utils.py:175-201, 252-274); either output
+ * may be NULL.  Float64 outputs computed from the FP32 points. */
+int dm_simplex_metrics(int32_t dim, const float *points, const int32_t *cells,
+                       int64_t nc, double *volume, double *quality,
+                       void *stream);
+
+/* laplacian2_fixed_point (geometry/utils.py:494-547) for 2D points
+ * float[n][2] (device, updated in place): interior vertices (boundary_flags
+ * 0) move to the solution of deg_i x_i - sum_j x_j = 0 with the boundary
+ * vertices fixed; Jacobi-preconditioned CG to relative residual rtol. */
+int dm_laplacian_workspace_size(int64_t n, size_t *bytes);
+int dm_laplacian_smooth(float *points, int64_t n, const int32_t *adj,
+                        int32_t adj_cap, const int32_t *deg,
+                        const int32_t *boundary_flags, int32_t max_iter,
+                        double rtol, int32_t *iters_host, void *workspace,
+                        size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMGB_H */

@@ -1,0 +1,167 @@
+"""ctypes binding of libdmgb.so (C ABI in include/dmgb.h).
+
+The CUDA library is the only compute path: if it cannot be loaded every
+operation raises instead of falling back to the CPU.
+"""
+import ctypes
+import os
+import threading
+
+from . import _build
+
+_lock = threading.Lock()
+_lib = None
+
+c_int = ctypes.c_int32
+c_i64 = ctypes.c_int64
+c_f = ctypes.c_float
+c_d = ctypes.c_double
+c_p = ctypes.c_void_p
+c_sz = ctypes.c_size_t
+
+DM_OK = 0
+DM_ERR_ARG = 1
+DM_ERR_CUDA = 2
+DM_ERR_CAPACITY = 3
+DM_ERR_NOT_CONVERGED = 4
+DM_ERR_DEGENERATE = 5
+DM_ERR_WORKSPACE = 6
+
+CNT_CELLS, CNT_ESCALATED, CNT_FLAGS, CNT_KEPT, CNT_EDGES, CNT_BAD, CNT_DUPS, CNT_AUX = range(8)
+NCOUNTERS = 16
+
+FLAG_CELL_OVERFLOW = 1
+FLAG_STAR_OVERFLOW = 2
+FLAG_SEED_FAILED = 4
+FLAG_DUPLICATES = 8
+FLAG_EXACT_OVERFLOW = 16
+FLAG_ADJ_OVERFLOW = 32
+FLAG_DIVERGED = 64
+FLAG_NONFINITE = 128
+
+SIZING_CONST, SIZING_GRID, SIZING_SLOTS = 0, 1, 2
+
+
+class SdfProgram(ctypes.Structure):
+    _fields_ = [("ops", c_p), ("params", c_p), ("n_ops", c_int), ("dim", c_int)]
+
+
+class Sizing(ctypes.Structure):
+    _fields_ = [
+        ("kind", c_int),
+        ("dim", c_int),
+        ("h", c_f),
+        ("grid", c_p),
+        ("n", c_int * 3),
+        ("lo", c_f * 3),
+        ("hi", c_f * 3),
+        ("slot_h", c_p),
+    ]
+
+
+_FP = ctypes.POINTER(c_f)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "dm_version": (c_int, []),
+    "dm_last_error": (ctypes.c_char_p, []),
+    "dm_abi_count": (c_int, []),
+    "dm_orient2": (c_int, [_FP, _FP, _FP]),
+    "dm_orient3": (c_int, [_FP, _FP, _FP, _FP]),
+    "dm_incircle_sos": (c_int, [_FP, _FP, _FP, _FP]),
+    "dm_insphere_sos": (c_int, [_FP, _FP, _FP, _FP, _FP]),
+    "dm_delaunay_workspace_size": (c_int, [c_int, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_delaunay": (c_int, [c_int, c_p, c_i64, c_p, c_i64, c_p, c_p, c_sz, c_p]),
+    "dm_filter_cells_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_filter_cells": (
+        c_int,
+        [c_int, c_p, c_p, c_i64, ctypes.POINTER(SdfProgram), c_f, c_p, c_p, c_p, c_sz, c_p],
+    ),
+    "dm_cell_centroids": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
+    "dm_adjacency": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_int, c_p, c_p, c_p]),
+    "dm_unique_edges_workspace_size": (c_int, [c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_unique_edges": (c_int, [c_p, c_i64, c_i64, c_p, ctypes.POINTER(c_i64), c_p, c_sz, c_p]),
+    "dm_bar_blocks": (c_int, [c_i64, ctypes.POINTER(c_int)]),
+    "dm_bar_sums": (c_int, [c_int, c_p, c_i64, c_p, c_int, c_p, ctypes.POINTER(Sizing), c_p, c_p]),
+    "dm_update_points": (
+        c_int,
+        [
+            c_int, c_p, c_p, c_i64, c_p, c_int, c_p, ctypes.POINTER(Sizing), c_p,
+            c_f, c_f, c_i64, ctypes.POINTER(SdfProgram), c_int, c_f, c_f, c_p, c_p,
+        ],
+    ),
+    "dm_slot_midpoints": (c_int, [c_int, c_p, c_i64, c_p, c_int, c_p, c_p, c_p]),
+    "dm_sdf_eval": (c_int, [ctypes.POINTER(SdfProgram), c_p, c_i64, c_int, c_p, c_p, c_p]),
+    "dm_sizing_eval": (c_int, [ctypes.POINTER(Sizing), c_p, c_i64, c_int, c_p, c_p]),
+    "dm_improve_level_set": (c_int, [c_int, c_p, c_p, c_i64, ctypes.POINTER(SdfProgram), c_f, c_p]),
+    "dm_dihedral_angles": (c_int, [c_p, c_p, c_i64, c_p, c_p]),
+    "dm_circumsphere_grad": (c_int, [c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
+    "dm_dihedral_flags": (c_int, [c_p, c_p, c_i64, c_int, c_f, c_f, c_p, c_p, c_p]),
+    "dm_sliver_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_sliver_perturb": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_p, c_f, c_p, c_sz, c_p, c_p]),
+    "dm_limgrad": (c_int, [ctypes.POINTER(c_int), c_d, c_d, c_int, c_p, c_p]),
+    "dm_boundary_workspace_size": (c_int, [c_int, c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_boundary": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_p, c_i64, c_p, c_p, c_sz, c_p]),
+    "dm_compact_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_compact_vertices": (
+        c_int,
+        [c_int, c_p, c_p, c_i64, c_p, c_i64, c_int, c_p, ctypes.POINTER(c_i64), c_p, c_sz, c_p],
+    ),
+    "dm_simplex_metrics": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
+    "dm_size_from_velocity": (
+        c_int,
+        [c_p, c_i64, c_i64, c_p, c_d, c_d, c_d, c_d, c_d, c_d, c_d, c_d, c_d, c_d,
+         c_int, c_p, ctypes.POINTER(c_int), c_p, c_sz, c_p],
+    ),
+    "dm_pad_grid": (
+        c_int,
+        [c_p, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+         c_int, c_int, c_d, c_p, c_p],
+    ),
+    "dm_laplacian_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_laplacian_smooth": (
+        c_int,
+        [c_p, c_i64, c_p, c_int, c_p, c_p, c_int, c_d, ctypes.POINTER(c_int), c_p, c_sz, c_p],
+    ),
+}
+
+
+class NativeError(RuntimeError):
+    def __init__(self, name, code, msg):
+        super().__init__(f"{name} failed with status {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Load libdmgb.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.library_path()
+        if not os.path.exists(path):
+            _build.build_library()
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def call(name, *args):
+    """Call an entry point and raise NativeError on a non-zero status."""
+    L = lib()
+    rc = getattr(L, name)(*args)
+    if rc != DM_OK:
+        msg = L.dm_last_error()
+        raise NativeError(name, rc, msg.decode() if msg else "")
+    return rc
+
+
+def fptr(arr):
+    """float* for a host numpy float32 array"""
+    return arr.ctypes.data_as(_FP)

@@ -1,0 +1,1703 @@
+// GPU Delaunay triangulation by independent vertex stars.
+//
+// Replaces the CGAL rebuild the reference performs every DistMesh iteration
+// (generation/mesh_generator.py:465-469 -> DelaunayTriangulation{,3}.insert,
+// generation/cpp/delaunay_class.cpp:108-121, delaunay_class3.cpp:116-129,
+// and get_finite_cells, delaunay_class.cpp:232-265, delaunay_class3.cpp:
+// 276-310).  The Delaunay triangulation of points in general position (and
+// of any point set under a fixed symbolic perturbation) is unique, so it can
+// be assembled from the stars of its vertices computed independently:
+//
+//   star(p) = all Delaunay cells incident to p.
+//
+// One warp computes one star by gift wrapping around p: starting from a
+// certified seed cell, every face through p is crossed by a query that
+// returns the point whose sphere through the face is smallest on the far
+// side (an insphere total order).  All predicates are exact (see
+// dm_predicates.cuh), so stars of different vertices agree and every cell is
+// emitted once, by its smallest vertex index.
+//
+// Level 1 runs the queries on the points within distance R of p, held in
+// shared memory.  A cell found this way whose circumball lies inside B(p, R)
+// is certified (every point that could invalidate it was examined).  A star
+// with an uncertified cell or an open (convex-hull) face is handed to level 2,
+// whose queries walk the uniform grid and its coarse blocks and are exact
+// over the whole point set.
+#include <float.h>
+
+#include "dm_common.cuh"
+#include "dm_predicates.cuh"
+
+namespace dm {
+
+using dmp::insph3_sos;
+using dmp::incirc2_sos;
+
+struct GridParams {
+  float lo[3];
+  float cs, inv_cs;
+  int dims[3];
+  int ncells;
+  int bs;  // coarse block edge (cells)
+  int bdims[3];
+  int nblocks;
+  int dim;
+};
+
+struct DTArgs {
+  int dim;
+  int64_t n;
+  const float *P;  // float4 (3D) or float2 (2D)
+  GridParams *gp;
+  int *bbox;          // 6 ordered ints
+  int32_t *cell_of;   // [n]
+  int32_t *slot;      // [n]
+  int32_t *cell_cnt;  // [cap_cells]
+  int32_t *cell_start;  // [cap_cells + 1]
+  int32_t *sorted;    // [n]
+  int32_t *scan_tmp;
+  int32_t *blk_cnt;   // [cap_blocks]
+  float *blk_box;     // [cap_blocks * 6]
+  uint8_t *dup;       // [n]
+  int32_t *esc;       // [n]
+  int4 *esc_seed;     // [n]
+  int32_t *cells;
+  int64_t cap_cells_out;
+  int64_t *counters;
+  int64_t cap_cells, cap_blocks;
+};
+
+static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
+  a.cap_cells = 2 * n + 4096;
+  a.cap_blocks = a.cap_cells;
+  a.gp = c.take<GridParams>(1);
+  a.bbox = c.take<int>(8);
+  a.cell_of = c.take<int32_t>(n);
+  a.slot = c.take<int32_t>(n);
+  a.cell_cnt = c.take<int32_t>(a.cap_cells);
+  a.cell_start = c.take<int32_t>(a.cap_cells + 1);
+  a.sorted = c.take<int32_t>(n);
+  a.scan_tmp = c.take<int32_t>(scan_tmp_elems(a.cap_cells));
+  a.blk_cnt = c.take<int32_t>(a.cap_blocks);
+  a.blk_box = c.take<float>(a.cap_blocks * 6);
+  a.dup = c.take<uint8_t>(n);
+  a.esc = c.take<int32_t>(n);
+  a.esc_seed = c.take<int4>(n);
+  return c.used;
+}
+
+// ---------------------------------------------------------------------------
+// point access
+template <int DIM>
+__device__ __forceinline__ void load_pt(const float *P, int i, float *x) {
+  if (DIM == 3) {
+    float4 v = __ldg(reinterpret_cast<const float4 *>(P) + i);
+    x[0] = v.x;
+    x[1] = v.y;
+    x[2] = v.z;
+  } else {
+    float2 v = __ldg(reinterpret_cast<const float2 *>(P) + i);
+    x[0] = v.x;
+    x[1] = v.y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// grid build
+__global__ void k_bbox_init(int *bbox) {
+  if (threadIdx.x < 3) {
+    bbox[threadIdx.x] = f2o(FLT_MAX);
+    bbox[3 + threadIdx.x] = f2o(-FLT_MAX);
+  }
+}
+
+template <int DIM>
+__global__ void k_bbox(const float *P, int64_t n, int *bbox, int64_t *counters) {
+  float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float x[3];
+    load_pt<DIM>(P, (int)i, x);
+    for (int k = 0; k < DIM; ++k) {
+      if (!isfinite(x[k])) bad = true;
+      mn[k] = fminf(mn[k], x[k]);
+      mx[k] = fmaxf(mx[k], x[k]);
+    }
+  }
+  for (int k = 0; k < DIM; ++k) {
+    for (int o = 16; o; o >>= 1) {
+      mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+      mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int k = 0; k < DIM; ++k) {
+      atomicMin(&bbox[k], f2o(mn[k]));
+      atomicMax(&bbox[3 + k], f2o(mx[k]));
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0)
+    flag_or(counters, DM_FLAG_NONFINITE);
+}
+
+__global__ void k_grid_params(GridParams *gp, const int *bbox, int64_t n,
+                              int dim, int64_t cap_cells, int64_t cap_blocks) {
+  if (threadIdx.x != 0) return;
+  double lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
+  double maxext = 0;
+  bool finite = true;
+  for (int k = 0; k < dim; ++k) {
+    lo[k] = o2f(bbox[k]);
+    double hi = o2f(bbox[3 + k]);
+    ext[k] = hi - lo[k];
+    if (!isfinite(lo[k]) || !isfinite(hi)) finite = false;
+    if (!(ext[k] >= 0) || !isfinite(ext[k])) ext[k] = 0;
+    maxext = fmax(maxext, ext[k]);
+  }
+  if (!finite) {
+    // non-finite input (already flagged): one cell, no triangulation work
+    for (int k = 0; k < dim; ++k) {
+      lo[k] = 0;
+      ext[k] = 0;
+    }
+    maxext = 0;
+  }
+  if (maxext <= 0) maxext = 1;
+  double vol = 1;
+  for (int k = 0; k < dim; ++k) vol *= fmax(ext[k], maxext * 1e-3);
+  double nn = (double)(n > 0 ? n : 1);
+  double cs = pow(vol / nn, 1.0 / dim);
+  if (!(cs > 0)) cs = maxext;
+  int dims[3] = {1, 1, 1};
+  for (int it = 0; it < 200; ++it) {
+    double cells = 1;
+    for (int k = 0; k < dim; ++k) {
+      double q = fmin(floor(ext[k] / cs), 1e9);
+      dims[k] = (int)q + 1;
+      cells *= dims[k];
+    }
+    if (cells <= (double)cap_cells) break;
+    cs *= 1.1;
+  }
+  // round cs up to a float that keeps floor((x-lo)/cs) within dims
+  GridParams g;
+  g.dim = dim;
+  g.cs = (float)cs;
+  g.inv_cs = (float)(1.0 / cs);
+  g.ncells = 1;
+  g.bs = dim == 3 ? 4 : 8;
+  g.nblocks = 1;
+  for (int k = 0; k < 3; ++k) {
+    g.lo[k] = k < dim ? (float)lo[k] : 0.f;
+    g.dims[k] = k < dim ? dims[k] : 1;
+    g.ncells *= g.dims[k];
+    g.bdims[k] = (g.dims[k] + g.bs - 1) / g.bs;
+    g.nblocks *= g.bdims[k];
+  }
+  *gp = g;
+}
+
+__device__ __forceinline__ int cell_coord(const GridParams &g, float x, int k) {
+  int c = (int)floorf((x - g.lo[k]) * g.inv_cs);
+  return min(max(c, 0), g.dims[k] - 1);
+}
+
+template <int DIM>
+__global__ void k_cell_count(const float *P, int64_t n, const GridParams *gp,
+                             int32_t *cell_of, int32_t *slot, int32_t *cnt) {
+  GridParams g = *gp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float x[3];
+    load_pt<DIM>(P, (int)i, x);
+    int c = cell_coord(g, x[0], 0) +
+            g.dims[0] * (cell_coord(g, x[1], 1) +
+                         (DIM == 3 ? g.dims[1] * cell_coord(g, x[2], 2) : 0));
+    cell_of[i] = c;
+    slot[i] = atomicAdd(&cnt[c], 1);
+  }
+}
+
+__global__ void k_cell_scatter(int64_t n, const int32_t *cell_of,
+                               const int32_t *slot, const int32_t *start,
+                               int32_t *sorted) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    sorted[start[cell_of[i]] + slot[i]] = (int32_t)i;
+}
+
+// sort each cell's points by index (deterministic order) and mark exact
+// duplicates: every point equal to a lower-index point gets dup = 1.
+template <int DIM>
+__global__ void k_cell_sort(const float *P, const GridParams *gp,
+                            const int32_t *start, int32_t *sorted,
+                            uint8_t *dup, int64_t *counters) {
+  int nc = gp->ncells;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += gridDim.x * blockDim.x) {
+    int b = start[c], e = start[c + 1];
+    for (int i = b + 1; i < e; ++i) {
+      int v = sorted[i], j = i - 1;
+      while (j >= b && sorted[j] > v) {
+        sorted[j + 1] = sorted[j];
+        --j;
+      }
+      sorted[j + 1] = v;
+    }
+    int ndup = 0;
+    for (int i = b; i < e; ++i) {
+      int vi = sorted[i];
+      float xi[3];
+      load_pt<DIM>(P, vi, xi);
+      uint8_t d = 0;
+      for (int j = b; j < i; ++j) {
+        float xj[3];
+        load_pt<DIM>(P, sorted[j], xj);
+        bool same = xi[0] == xj[0] && xi[1] == xj[1] && (DIM == 2 || xi[2] == xj[2]);
+        if (same) {
+          d = 1;
+          break;
+        }
+      }
+      dup[vi] = d;
+      ndup += d;
+    }
+    if (ndup) {
+      atomicAdd((unsigned long long *)&counters[DM_CNT_DUPS], (unsigned long long)ndup);
+      flag_or(counters, DM_FLAG_DUPLICATES);
+    }
+  }
+}
+
+template <int DIM>
+__global__ void k_block_boxes(const float *P, const GridParams *gp,
+                              const int32_t *start, const int32_t *sorted,
+                              int32_t *blk_cnt, float *blk_box) {
+  GridParams g = *gp;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < g.nblocks;
+       b += gridDim.x * blockDim.x) {
+    int bx = b % g.bdims[0], by = (b / g.bdims[0]) % g.bdims[1],
+        bz = b / (g.bdims[0] * g.bdims[1]);
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    int cnt = 0;
+    int z0 = DIM == 3 ? bz * g.bs : 0, z1 = DIM == 3 ? min(z0 + g.bs, g.dims[2]) : 1;
+    for (int cz = z0; cz < z1; ++cz)
+      for (int cy = by * g.bs; cy < min(by * g.bs + g.bs, g.dims[1]); ++cy)
+        for (int cx = bx * g.bs; cx < min(bx * g.bs + g.bs, g.dims[0]); ++cx) {
+          int c = cx + g.dims[0] * (cy + g.dims[1] * cz);
+          for (int i = start[c]; i < start[c + 1]; ++i) {
+            float x[3];
+            load_pt<DIM>(P, sorted[i], x);
+            for (int k = 0; k < DIM; ++k) {
+              mn[k] = fminf(mn[k], x[k]);
+              mx[k] = fmaxf(mx[k], x[k]);
+            }
+            ++cnt;
+          }
+        }
+    blk_cnt[b] = cnt;
+    for (int k = 0; k < 3; ++k) {
+      blk_box[6 * b + k] = mn[k];
+      blk_box[6 * b + 3 + k] = mx[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Level 1: shared-memory neighbourhoods
+template <int DIM>
+struct L1 {};
+template <>
+struct L1<3> {
+  static constexpr int CAP = 128, PER = 4, K = 2, MAXTRI = 128, MAXOPEN = 96;
+};
+template <>
+struct L1<2> {
+  static constexpr int CAP = 64, PER = 2, K = 3, MAXTRI = 64, MAXOPEN = 4;
+};
+
+constexpr int L1_WARPS = 4;
+
+template <int DIM>
+struct WarpL1 {
+  float4 c[L1<DIM>::CAP];  // relative coords (x,y,z) and lift (w)
+  int id[L1<DIM>::CAP];    // global index
+  uint32_t tri[L1<DIM>::MAXTRI];
+  uint32_t open[L1<DIM>::MAXOPEN];
+  int nc, ntri, nopen;
+  int flags;
+  float reff;
+};
+
+__device__ __forceinline__ uint32_t pack3(int a, int b, int c) {
+  return (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16);
+}
+__device__ __forceinline__ int un0(uint32_t t) { return t & 0xff; }
+__device__ __forceinline__ int un1(uint32_t t) { return (t >> 8) & 0xff; }
+__device__ __forceinline__ int un2(uint32_t t) { return (t >> 16) & 0xff; }
+
+// warp argmin over (key, id); lanes with no candidate pass key=+inf, j=-1
+__device__ __forceinline__ void warp_argmin(float &key, int &j, int &gid) {
+  for (int o = 16; o; o >>= 1) {
+    float k2 = __shfl_xor_sync(0xffffffffu, key, o);
+    int j2 = __shfl_xor_sync(0xffffffffu, j, o);
+    int g2 = __shfl_xor_sync(0xffffffffu, gid, o);
+    bool take = (j2 >= 0) && (j < 0 || k2 < key || (k2 == key && g2 < gid));
+    if (take) {
+      key = k2;
+      j = j2;
+      gid = g2;
+    }
+  }
+}
+
+// ---- 3D level-1 predicates on shared candidates (p is the origin)
+__device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
+                                   int a, int b, int c) {
+  float4 A = S.c[a], B = S.c[b], C = S.c[c];
+  int s = dmp::orient3_rel_filter<float>(A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
+                                         C.z, 16.0f * DMP_U32);
+  if (s) return s;
+  float pr[3], ar[3], br[3], cr[3];
+  load_pt<3>(P, ip, pr);
+  load_pt<3>(P, S.id[a], ar);
+  load_pt<3>(P, S.id[b], br);
+  load_pt<3>(P, S.id[c], cr);
+  return dmp::orient3_slow(pr, ar, br, cr);
+}
+
+__device__ __forceinline__ int is3L(const WarpL1<3> &S, const float *P, int ip,
+                                    int a, int b, int c, int d, int &ovf) {
+  float4 A = S.c[a], B = S.c[b], C = S.c[c], D = S.c[d];
+  float X[3] = {A.x, A.y, A.z}, Y[3] = {B.x, B.y, B.z}, Z[3] = {C.x, C.y, C.z},
+        W[3] = {D.x, D.y, D.z};
+  int s = dmp::insph3_rel_filter<float>(X, Y, Z, W, A.w, B.w, C.w, D.w,
+                                        48.0f * DMP_U32);
+  if (s) return s;
+  float pr[3], ar[3], br[3], cr[3], dr[3];
+  load_pt<3>(P, ip, pr);
+  load_pt<3>(P, S.id[a], ar);
+  load_pt<3>(P, S.id[b], br);
+  load_pt<3>(P, S.id[c], cr);
+  load_pt<3>(P, S.id[d], dr);
+  return insph3_sos(pr, ar, br, cr, dr, &ovf);
+}
+
+// gift-wrap query on face (p, a, b): winner among candidates y with
+// orient3(p,a,b,y) > 0 whose sphere through the face is smallest; -1 if none.
+__device__ int gw3L(const WarpL1<3> &S, const float *P, int ip, int a, int b,
+                    int lane, int &ovf) {
+  const int nc = S.nc;
+  float4 A = S.c[a], B = S.c[b];
+  float nx = A.y * B.z - A.z * B.y, ny = A.z * B.x - A.x * B.z,
+        nz = A.x * B.y - A.y * B.x;
+  float nn = nx * nx + ny * ny + nz * nz;
+  float tx = A.w * B.x - B.w * A.x, ty = A.w * B.y - B.w * A.y,
+        tz = A.w * B.z - B.w * A.z;
+  float inv = nn > 0.f ? 0.5f / nn : 0.f;
+  float cx = (ty * nz - tz * ny) * inv, cy = (tz * nx - tx * nz) * inv,
+        cz = (tx * ny - ty * nx) * inv;
+  uint32_t pos = 0;
+  float bk = FLT_MAX;
+  int bj = -1, bg = 0x7fffffff;
+#pragma unroll
+  for (int s = 0; s < L1<3>::PER; ++s) {
+    int j = lane + 32 * s;
+    if (j < nc && j != a && j != b) {
+      if (o3L(S, P, ip, a, b, j) > 0) {
+        pos |= 1u << s;
+        float4 Y = S.c[j];
+        float den = Y.x * nx + Y.y * ny + Y.z * nz;
+        float tau = (Y.w - 2.f * (Y.x * cx + Y.y * cy + Y.z * cz)) / den;
+        if (!(tau == tau) || !(den > 0.f)) tau = FLT_MAX;
+        int g = S.id[j];
+        if (bj < 0 || tau < bk || (tau == bk && g < bg)) {
+          bk = tau;
+          bj = j;
+          bg = g;
+        }
+      }
+    }
+  }
+  warp_argmin(bk, bj, bg);
+  if (bj < 0) return -1;
+  for (int it = 0; it < nc + 1; ++it) {
+    int found = -1;
+#pragma unroll
+    for (int s = 0; s < L1<3>::PER; ++s) {
+      int j = lane + 32 * s;
+      if (found < 0 && (pos >> s & 1u) && j != bj) {
+        if (is3L(S, P, ip, a, b, bj, j, ovf) < 0) found = j;
+      }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, found >= 0);
+    if (!m) return bj;
+    bj = __shfl_sync(0xffffffffu, found, __ffs(m) - 1);
+  }
+  return bj;
+}
+
+// find open edge (t -> s) (reverse of s -> t); returns index or -1
+template <int DIM>
+__device__ __forceinline__ int find_rev(const WarpL1<DIM> &S, int s, int t,
+                                        int lane) {
+  int hit = -1;
+  for (int k = lane; k < S.nopen; k += 32) {
+    uint32_t e = S.open[k];
+    if (un0(e) == t && un1(e) == s) hit = k;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, hit >= 0);
+  if (!m) return -1;
+  return __shfl_sync(0xffffffffu, hit, __ffs(m) - 1);
+}
+
+// circumball of cell (p, A, B, C) inside B(p, reff)?  Requires a well
+// conditioned orientation so the float circumradius is trustworthy.
+__device__ __forceinline__ bool certified3(float4 A, float4 B, float4 C,
+                                           float reff) {
+  float bcx = B.y * C.z - B.z * C.y, bcy = B.z * C.x - B.x * C.z,
+        bcz = B.x * C.y - B.y * C.x;
+  float cax = C.y * A.z - C.z * A.y, cay = C.z * A.x - C.x * A.z,
+        caz = C.x * A.y - C.y * A.x;
+  float abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z,
+        abz = A.x * B.y - A.y * B.x;
+  float det = A.x * bcx + A.y * bcy + A.z * bcz;
+  float perm = fabsf(A.x) * (fabsf(B.y * C.z) + fabsf(B.z * C.y)) +
+               fabsf(A.y) * (fabsf(B.z * C.x) + fabsf(B.x * C.z)) +
+               fabsf(A.z) * (fabsf(B.x * C.y) + fabsf(B.y * C.x));
+  if (!(fabsf(det) > 1e4f * 16.0f * DMP_U32 * perm)) return false;
+  float nx = A.w * bcx + B.w * cax + C.w * abx;
+  float ny = A.w * bcy + B.w * cay + C.w * aby;
+  float nz = A.w * bcz + B.w * caz + C.w * abz;
+  float num2 = nx * nx + ny * ny + nz * nz;  // (2 r det)^2 * ... = 4 r^2 det^2
+  float lim = 0.99f * reff;
+  return num2 <= lim * lim * det * det;
+}
+
+template <int DIM>
+__device__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const GridParams &g,
+                          int ip, const float *px, int lane) {
+  constexpr int K = L1<DIM>::K, W = 2 * K + 1;
+  constexpr int NCELL = DIM == 3 ? W * W * W : W * W;
+  int cc[3];
+  for (int k = 0; k < DIM; ++k) cc[k] = cell_coord(g, px[k], k);
+  // covered radius: distance from p to the faces of the block of cells
+  float rcov = FLT_MAX;
+  for (int k = 0; k < DIM; ++k) {
+    if (cc[k] - K > 0) rcov = fminf(rcov, px[k] - (g.lo[k] + (cc[k] - K) * g.cs));
+    if (cc[k] + K + 1 < g.dims[k])
+      rcov = fminf(rcov, (g.lo[k] + (cc[k] + K + 1) * g.cs) - px[k]);
+  }
+  rcov = rcov * (1.f - 1e-5f);
+  if (rcov > 1e30f) rcov = 1e30f;
+  float rc2 = rcov * rcov;
+  // pass 1: count, with a 16-bin histogram of d / rcov
+  int bins[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) bins[k] = 0;
+  int total = 0;
+  for (int t = lane; t < NCELL; t += 32) {
+    int d0 = t % W - K, d1 = (t / W) % W - K, d2 = DIM == 3 ? t / (W * W) - K : 0;
+    int x = cc[0] + d0, y = cc[1] + d1, z = DIM == 3 ? cc[2] + d2 : 0;
+    if (x < 0 || y < 0 || z < 0 || x >= g.dims[0] || y >= g.dims[1] ||
+        (DIM == 3 && z >= g.dims[2]))
+      continue;
+    int c = x + g.dims[0] * (y + g.dims[1] * z);
+    for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) {
+      int q = A.sorted[i];
+      if (q == ip || A.dup[q]) continue;
+      float xq[3];
+      load_pt<DIM>(A.P, q, xq);
+      float d2s = 0.f;
+      for (int k = 0; k < DIM; ++k) {
+        float dd = xq[k] - px[k];
+        d2s += dd * dd;
+      }
+      if (d2s <= rc2) {
+        ++total;
+        int bidx = min(15, (int)(sqrtf(d2s) / rcov * 16.f));
+        for (int k = 0; k < 16; ++k) bins[k] += (k == bidx);
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+  int bmax = 15;
+  float reff = rcov;
+  if (total > L1<DIM>::CAP) {
+    int cum = 0;
+    bmax = -1;
+    for (int k = 0; k < 16; ++k) {
+      int v = bins[k];
+      for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      cum += v;
+      if (cum <= L1<DIM>::CAP) bmax = k;
+    }
+    reff = rcov * (bmax + 1) / 16.f * (1.f - 1e-5f);
+  }
+  if (lane == 0) {
+    S.nc = 0;
+    S.reff = bmax < 0 ? 0.f : reff;
+  }
+  __syncwarp();
+  if (bmax < 0) return;
+  // pass 2: collect
+  for (int t = lane; t < NCELL; t += 32) {
+    int d0 = t % W - K, d1 = (t / W) % W - K, d2 = DIM == 3 ? t / (W * W) - K : 0;
+    int x = cc[0] + d0, y = cc[1] + d1, z = DIM == 3 ? cc[2] + d2 : 0;
+    if (x < 0 || y < 0 || z < 0 || x >= g.dims[0] || y >= g.dims[1] ||
+        (DIM == 3 && z >= g.dims[2]))
+      continue;
+    int c = x + g.dims[0] * (y + g.dims[1] * z);
+    for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) {
+      int q = A.sorted[i];
+      if (q == ip || A.dup[q]) continue;
+      float xq[3];
+      load_pt<DIM>(A.P, q, xq);
+      float r[3] = {0, 0, 0}, d2s = 0.f;
+      for (int k = 0; k < DIM; ++k) {
+        r[k] = xq[k] - px[k];
+        d2s += r[k] * r[k];
+      }
+      if (d2s > rc2) continue;
+      int bidx = min(15, (int)(sqrtf(d2s) / rcov * 16.f));
+      if (bidx > bmax) continue;
+      int slot = atomicAdd(&S.nc, 1);
+      if (slot < L1<DIM>::CAP) {
+        S.c[slot] = make_float4(r[0], r[1], r[2],
+                                DIM == 3 ? r[0] * r[0] + r[1] * r[1] + r[2] * r[2]
+                                         : r[0] * r[0] + r[1] * r[1]);
+        S.id[slot] = q;
+      }
+    }
+  }
+  __syncwarp();
+  if (lane == 0 && S.nc > L1<DIM>::CAP) S.nc = L1<DIM>::CAP;  // cannot happen
+  __syncwarp();
+}
+
+// seed search (3D): returns packed link triangle or 0xffffffff
+__device__ uint32_t seed3L(const WarpL1<3> &S, const float *P, int ip, int lane,
+                           int &ovf) {
+  const int nc = S.nc;
+  float pk1 = -1.f;
+  int pg1 = -1;
+  for (int t1 = 0; t1 < 3; ++t1) {
+    // next nearest after (pk1, pg1)
+    float bk = FLT_MAX;
+    int bj = -1, bg = 0x7fffffff;
+    for (int s = 0; s < L1<3>::PER; ++s) {
+      int j = lane + 32 * s;
+      if (j >= nc) continue;
+      float k = S.c[j].w;
+      int g = S.id[j];
+      bool after = k > pk1 || (k == pk1 && g > pg1);
+      if (after && (bj < 0 || k < bk || (k == bk && g < bg))) {
+        bk = k;
+        bj = j;
+        bg = g;
+      }
+    }
+    warp_argmin(bk, bj, bg);
+    if (bj < 0) return 0xffffffffu;
+    int q1 = bj;
+    pk1 = bk;
+    pg1 = bg;
+    float4 Q = S.c[q1];
+    float pk2 = -1.f;
+    int pg2 = -1;
+    for (int t2 = 0; t2 < 6; ++t2) {
+      float ck = FLT_MAX;
+      int cj = -1, cg = 0x7fffffff;
+      for (int s = 0; s < L1<3>::PER; ++s) {
+        int j = lane + 32 * s;
+        if (j >= nc || j == q1) continue;
+        float4 Y = S.c[j];
+        float cx = Q.y * Y.z - Q.z * Y.y, cy = Q.z * Y.x - Q.x * Y.z,
+              cz = Q.x * Y.y - Q.y * Y.x;
+        float cr = cx * cx + cy * cy + cz * cz;
+        if (!(cr > 0.f)) continue;
+        float dx = Q.x - Y.x, dy = Q.y - Y.y, dz = Q.z - Y.z;
+        float k = Q.w * Y.w * (dx * dx + dy * dy + dz * dz) / cr;
+        int g = S.id[j];
+        bool after = k > pk2 || (k == pk2 && g > pg2);
+        if (after && (cj < 0 || k < ck || (k == ck && g < cg))) {
+          ck = k;
+          cj = j;
+          cg = g;
+        }
+      }
+      warp_argmin(ck, cj, cg);
+      if (cj < 0) break;
+      pk2 = ck;
+      pg2 = cg;
+      int q2 = cj;
+      int xp = gw3L(S, P, ip, q1, q2, lane, ovf);
+      int xm = gw3L(S, P, ip, q2, q1, lane, ovf);
+      if (xp < 0 && xm < 0) continue;
+      bool ok = true;
+      if (xp >= 0 && xm >= 0) ok = is3L(S, P, ip, q1, q2, xp, xm, ovf) > 0;
+      if (ok) return xp >= 0 ? pack3(q1, q2, xp) : pack3(q2, q1, xm);
+    }
+  }
+  return 0xffffffffu;
+}
+
+// seed search (2D): link edge (a, b) of a positive triangle (p, a, b)
+__device__ int gw2L(const WarpL1<2> &S, const float *P, int ip, int x, int sgn,
+                    int lane, int &ovf);
+
+__device__ __forceinline__ int o2L(const WarpL1<2> &S, const float *P, int ip,
+                                   int a, int b) {
+  float4 A = S.c[a], B = S.c[b];
+  int s = dmp::orient2_rel_filter<float>(A.x, A.y, B.x, B.y, 8.0f * DMP_U32);
+  if (s) return s;
+  float pr[2], ar[2], br[2];
+  load_pt<2>(P, ip, pr);
+  load_pt<2>(P, S.id[a], ar);
+  load_pt<2>(P, S.id[b], br);
+  return dmp::orient2_slow(pr, ar, br);
+}
+
+// incirc2(p, a, b, d)
+__device__ __forceinline__ int ic2L(const WarpL1<2> &S, const float *P, int ip,
+                                    int a, int b, int d, int &ovf) {
+  float4 A = S.c[a], B = S.c[b], D = S.c[d];
+  float X[2] = {A.x, A.y}, Y[2] = {B.x, B.y}, Z[2] = {D.x, D.y};
+  int s = dmp::incirc2_rel_filter<float>(X, Y, Z, A.w, B.w, D.w, 16.0f * DMP_U32);
+  if (s) return s;
+  float pr[2], ar[2], br[2], dr[2];
+  load_pt<2>(P, ip, pr);
+  load_pt<2>(P, S.id[a], ar);
+  load_pt<2>(P, S.id[b], br);
+  load_pt<2>(P, S.id[d], dr);
+  return incirc2_sos(pr, ar, br, dr, &ovf);
+}
+
+// 2D gift-wrap across edge (p, x): sgn=+1 candidates with orient2(p,x,y)>0
+// (triangle (p,x,y)); sgn=-1 candidates with orient2(p,y,x)>0 (triangle
+// (p,y,x)).  Winner has the smallest circle through p and x on that side.
+__device__ int gw2L(const WarpL1<2> &S, const float *P, int ip, int x, int sgn,
+                    int lane, int &ovf) {
+  const int nc = S.nc;
+  float4 X = S.c[x];
+  float nx = -X.y * sgn, ny = X.x * sgn;
+  uint32_t pos = 0;
+  float bk = FLT_MAX;
+  int bj = -1, bg = 0x7fffffff;
+#pragma unroll
+  for (int s = 0; s < L1<2>::PER; ++s) {
+    int j = lane + 32 * s;
+    if (j < nc && j != x) {
+      int o = sgn > 0 ? o2L(S, P, ip, x, j) : o2L(S, P, ip, j, x);
+      if (o > 0) {
+        pos |= 1u << s;
+        float4 Y = S.c[j];
+        float den = Y.x * nx + Y.y * ny;
+        float tau = (Y.w - (Y.x * X.x + Y.y * X.y)) / den;
+        if (!(tau == tau) || !(den > 0.f)) tau = FLT_MAX;
+        int g = S.id[j];
+        if (bj < 0 || tau < bk || (tau == bk && g < bg)) {
+          bk = tau;
+          bj = j;
+          bg = g;
+        }
+      }
+    }
+  }
+  warp_argmin(bk, bj, bg);
+  if (bj < 0) return -1;
+  for (int it = 0; it < nc + 1; ++it) {
+    int found = -1;
+#pragma unroll
+    for (int s = 0; s < L1<2>::PER; ++s) {
+      int j = lane + 32 * s;
+      if (found < 0 && (pos >> s & 1u) && j != bj) {
+        int r = sgn > 0 ? ic2L(S, P, ip, x, bj, j, ovf) : ic2L(S, P, ip, bj, x, j, ovf);
+        if (r < 0) found = j;
+      }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, found >= 0);
+    if (!m) return bj;
+    bj = __shfl_sync(0xffffffffu, found, __ffs(m) - 1);
+  }
+  return bj;
+}
+
+__device__ __forceinline__ bool certified2(float4 A, float4 B, float reff) {
+  float det = A.x * B.y - A.y * B.x;
+  float perm = fabsf(A.x * B.y) + fabsf(A.y * B.x);
+  if (!(fabsf(det) > 1e4f * 8.0f * DMP_U32 * perm)) return false;
+  float nx = B.y * A.w - A.y * B.w, ny = A.x * B.w - B.x * A.w;
+  float lim = 0.99f * reff;
+  return nx * nx + ny * ny <= lim * lim * det * det;
+}
+
+// 2D seed: returns packed (q1, x) with triangle (p, q1, x) positive, or ~0
+__device__ uint32_t seed2L(const WarpL1<2> &S, const float *P, int ip, int lane,
+                           int &ovf) {
+  const int nc = S.nc;
+  float pk = -1.f;
+  int pg = -1;
+  for (int t = 0; t < 6; ++t) {
+    float bk = FLT_MAX;
+    int bj = -1, bg = 0x7fffffff;
+    for (int s = 0; s < L1<2>::PER; ++s) {
+      int j = lane + 32 * s;
+      if (j >= nc) continue;
+      float k = S.c[j].w;
+      int g = S.id[j];
+      bool after = k > pk || (k == pk && g > pg);
+      if (after && (bj < 0 || k < bk || (k == bk && g < bg))) {
+        bk = k;
+        bj = j;
+        bg = g;
+      }
+    }
+    warp_argmin(bk, bj, bg);
+    if (bj < 0) return 0xffffffffu;
+    pk = bk;
+    pg = bg;
+    int q1 = bj;
+    int xp = gw2L(S, P, ip, q1, +1, lane, ovf);
+    int xm = gw2L(S, P, ip, q1, -1, lane, ovf);
+    if (xp < 0 && xm < 0) continue;
+    bool ok = true;
+    if (xp >= 0 && xm >= 0) ok = ic2L(S, P, ip, q1, xp, xm, ovf) > 0;
+    if (ok) return xp >= 0 ? pack3(q1, xp, 0) : pack3(xm, q1, 0);
+  }
+  return 0xffffffffu;
+}
+
+// escalation record: (p, a, b, c) global ids; c < 0 means "no seed";
+// bit 30 of p marks a certified seed cell.
+__device__ __forceinline__ void escalate(const DTArgs &A, int p, int4 seed,
+                                         int lane) {
+  int64_t k = warp_append(&A.counters[DM_CNT_ESCALATED], lane == 0);
+  if (lane == 0) {
+    A.esc[k] = p;
+    A.esc_seed[k] = seed;
+  }
+}
+
+__global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
+  __shared__ WarpL1<3> sm[L1_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpL1<3> &S = sm[w];
+  const GridParams g = *A.gp;
+  for (int64_t pv = (int64_t)blockIdx.x * L1_WARPS + w; pv < A.n;
+       pv += (int64_t)gridDim.x * L1_WARPS) {
+    const int ip = (int)pv;
+    if (A.dup[ip]) continue;
+    float px[3];
+    load_pt<3>(A.P, ip, px);
+    gather_l1<3>(S, A, g, ip, px, lane);
+    int ovf = 0;
+    uint32_t seed = S.nc >= 3 ? seed3L(S, A.P, ip, lane, ovf) : 0xffffffffu;
+    if (seed == 0xffffffffu) {
+      escalate(A, ip, make_int4(ip, -1, -1, -1), lane);
+      continue;
+    }
+    if (lane == 0) {
+      S.ntri = 1;
+      S.tri[0] = seed;
+      int a = un0(seed), b = un1(seed), c = un2(seed);
+      S.open[0] = pack3(a, b, c);
+      S.open[1] = pack3(b, c, a);
+      S.open[2] = pack3(c, a, b);
+      S.nopen = 3;
+      S.flags = 0;
+    }
+    __syncwarp();
+    int hull = 0;
+    while (S.nopen > 0) {
+      uint32_t e = S.open[S.nopen - 1];
+      __syncwarp();
+      if (lane == 0) S.nopen--;
+      __syncwarp();
+      int u = un0(e), v = un1(e);
+      int y = gw3L(S, A.P, ip, v, u, lane, ovf);
+      if (y < 0) {
+        hull = 1;
+        continue;
+      }
+      if (S.ntri >= L1<3>::MAXTRI) {
+        if (lane == 0) S.flags |= 1;
+        __syncwarp();
+        break;
+      }
+      if (lane == 0) S.tri[S.ntri++] = pack3(v, u, y);
+      __syncwarp();
+      // new directed edges (u, y | v) and (y, v | u)
+      int es[2][3] = {{u, y, v}, {y, v, u}};
+      for (int k = 0; k < 2; ++k) {
+        int r = find_rev<3>(S, es[k][0], es[k][1], lane);
+        if (lane == 0) {
+          if (r >= 0) {
+            S.open[r] = S.open[S.nopen - 1];
+            S.nopen--;
+          } else if (S.nopen < L1<3>::MAXOPEN) {
+            S.open[S.nopen++] = pack3(es[k][0], es[k][1], es[k][2]);
+          } else {
+            S.flags |= 1;
+          }
+        }
+        __syncwarp();
+      }
+      if (S.flags) break;
+    }
+    // certification
+    bool allok = !hull && !S.flags;
+    int cert_any = -1;
+    for (int t = lane; t < S.ntri; t += 32) {
+      uint32_t tr = S.tri[t];
+      bool ok = certified3(S.c[un0(tr)], S.c[un1(tr)], S.c[un2(tr)], S.reff);
+      if (!ok) allok = false;
+      else if (cert_any < 0) cert_any = t;
+    }
+    allok = __all_sync(0xffffffffu, allok);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    if (!allok) {
+      unsigned m = __ballot_sync(0xffffffffu, cert_any >= 0);
+      int4 sd;
+      if (m) {
+        int t = __shfl_sync(0xffffffffu, cert_any, __ffs(m) - 1);
+        uint32_t tr = S.tri[t];
+        sd = make_int4(ip | (1 << 30), S.id[un0(tr)], S.id[un1(tr)], S.id[un2(tr)]);
+      } else {
+        uint32_t tr = S.tri[0];
+        sd = make_int4(ip, S.id[un0(tr)], S.id[un1(tr)], S.id[un2(tr)]);
+      }
+      escalate(A, ip, sd, lane);
+      continue;
+    }
+    // emit cells owned by p (p has the smallest index)
+    for (int t0 = 0; t0 < S.ntri; t0 += 32) {
+      int t = t0 + lane;
+      bool own = false;
+      int ga = 0, gb = 0, gc = 0;
+      if (t < S.ntri) {
+        uint32_t tr = S.tri[t];
+        ga = S.id[un0(tr)];
+        gb = S.id[un1(tr)];
+        gc = S.id[un2(tr)];
+        own = ip < ga && ip < gb && ip < gc;
+      }
+      int64_t k = warp_append(&A.counters[DM_CNT_CELLS], own);
+      if (own) {
+        if (k < A.cap_cells_out) {
+          int4 *out = reinterpret_cast<int4 *>(A.cells);
+          out[k] = make_int4(ip, ga, gb, gc);
+        } else {
+          flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
+  __shared__ WarpL1<2> sm[L1_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpL1<2> &S = sm[w];
+  const GridParams g = *A.gp;
+  for (int64_t pv = (int64_t)blockIdx.x * L1_WARPS + w; pv < A.n;
+       pv += (int64_t)gridDim.x * L1_WARPS) {
+    const int ip = (int)pv;
+    if (A.dup[ip]) continue;
+    float px[2];
+    load_pt<2>(A.P, ip, px);
+    gather_l1<2>(S, A, g, ip, px, lane);
+    int ovf = 0;
+    uint32_t seed = S.nc >= 2 ? seed2L(S, A.P, ip, lane, ovf) : 0xffffffffu;
+    if (seed == 0xffffffffu) {
+      escalate(A, ip, make_int4(ip, -1, -1, -1), lane);
+      continue;
+    }
+    // forward walk: v0 = a, v1 = b, v_{i+1} = gw(v_i, +1) until closed
+    int a = un0(seed), b = un1(seed);
+    if (lane == 0) {
+      S.ntri = 1;
+      S.tri[0] = pack3(a, b, 0);
+      S.flags = 0;
+    }
+    __syncwarp();
+    bool closed = false, hull = false;
+    int cur = b;
+    while (true) {
+      int nx = gw2L(S, A.P, ip, cur, +1, lane, ovf);
+      if (nx < 0) {
+        hull = true;
+        break;
+      }
+      if (nx == a) {
+        closed = true;
+        break;
+      }
+      if (S.ntri >= L1<2>::MAXTRI) {
+        if (lane == 0) S.flags |= 1;
+        __syncwarp();
+        break;
+      }
+      if (lane == 0) S.tri[S.ntri++] = pack3(cur, nx, 0);
+      __syncwarp();
+      cur = nx;
+    }
+    if (hull && !S.flags) {
+      cur = a;
+      while (true) {
+        int pv2 = gw2L(S, A.P, ip, cur, -1, lane, ovf);
+        if (pv2 < 0) break;
+        if (S.ntri >= L1<2>::MAXTRI) {
+          if (lane == 0) S.flags |= 1;
+          __syncwarp();
+          break;
+        }
+        if (lane == 0) S.tri[S.ntri++] = pack3(pv2, cur, 0);
+        __syncwarp();
+        cur = pv2;
+      }
+    }
+    (void)closed;
+    bool allok = !hull && !S.flags;
+    int cert_any = -1;
+    for (int t = lane; t < S.ntri; t += 32) {
+      uint32_t tr = S.tri[t];
+      bool ok = certified2(S.c[un0(tr)], S.c[un1(tr)], S.reff);
+      if (!ok) allok = false;
+      else if (cert_any < 0) cert_any = t;
+    }
+    allok = __all_sync(0xffffffffu, allok);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    if (!allok) {
+      unsigned m = __ballot_sync(0xffffffffu, cert_any >= 0);
+      int4 sd;
+      int t = m ? __shfl_sync(0xffffffffu, cert_any, __ffs(m) - 1) : 0;
+      uint32_t tr = S.tri[t];
+      sd = make_int4(ip | (m ? (1 << 30) : 0), S.id[un0(tr)], S.id[un1(tr)], 0);
+      escalate(A, ip, sd, lane);
+      continue;
+    }
+    for (int t0 = 0; t0 < S.ntri; t0 += 32) {
+      int t = t0 + lane;
+      bool own = false;
+      int ga = 0, gb = 0;
+      if (t < S.ntri) {
+        uint32_t tr = S.tri[t];
+        ga = S.id[un0(tr)];
+        gb = S.id[un1(tr)];
+        own = ip < ga && ip < gb;
+      }
+      int64_t k = warp_append(&A.counters[DM_CNT_CELLS], own);
+      if (own) {
+        if (k < A.cap_cells_out) {
+          A.cells[3 * k] = ip;
+          A.cells[3 * k + 1] = ga;
+          A.cells[3 * k + 2] = gb;
+        } else {
+          flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Level 2: exhaustive queries over the grid
+constexpr int L2_WARPS = 4;
+constexpr int L2_MAXTRI = 192, L2_MAXOPEN = 128;
+
+struct WarpL2 {
+  int3 tri[L2_MAXTRI];
+  int3 open[L2_MAXOPEN];
+  int ntri, nopen, flags;
+};
+
+struct GQ {
+  const DTArgs *A;
+  GridParams g;
+};
+
+template <int DIM>
+__device__ __forceinline__ void ldp(const DTArgs &A, int i, float *x) {
+  load_pt<DIM>(A.P, i, x);
+}
+
+// 3D: compare candidate j against current best on face (p,a,b)
+struct Face3 {
+  int ip, ia, ib;
+  float p[3], a[3], b[3];
+  float V[3], U[3], n[3];
+};
+
+__device__ __forceinline__ int side3(const Face3 &F, const float *y) {
+  float Y[3] = {y[0] - F.p[0], y[1] - F.p[1], y[2] - F.p[2]};
+  int s = dmp::orient3_rel_filter<float>(F.V[0], F.V[1], F.V[2], F.U[0], F.U[1],
+                                         F.U[2], Y[0], Y[1], Y[2], 16.0f * DMP_U32);
+  if (s) return s;
+  return dmp::orient3_slow(F.p, F.a, F.b, y);
+}
+
+__device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j,
+                                          int &best, float *bx, int &ovf) {
+  if (j == F.ip || j == F.ia || j == F.ib || A.dup[j]) return;
+  float y[3];
+  load_pt<3>(A.P, j, y);
+  if (side3(F, y) <= 0) return;
+  if (best < 0 || insph3_sos(F.p, F.a, F.b, bx, y, &ovf) < 0) {
+    best = j;
+    bx[0] = y[0];
+    bx[1] = y[1];
+    bx[2] = y[2];
+  }
+}
+
+__device__ __forceinline__ int tourney3(const DTArgs &A, const Face3 &F,
+                                        int best, int &ovf) {
+  for (int o = 16; o; o >>= 1) {
+    int other = __shfl_xor_sync(0xffffffffu, best, o);
+    if (other >= 0 && other != best) {
+      if (best < 0) {
+        best = other;
+      } else {
+        float bx[3], ox[3];
+        load_pt<3>(A.P, best, bx);
+        load_pt<3>(A.P, other, ox);
+        if (insph3_sos(F.p, F.a, F.b, bx, ox, &ovf) < 0) best = other;
+      }
+    }
+  }
+  return best;
+}
+
+__device__ __forceinline__ bool in_local(const int *cc, int x, int y, int z,
+                                         int dim) {
+  return abs(x - cc[0]) <= 1 && abs(y - cc[1]) <= 1 && (dim == 2 || abs(z - cc[2]) <= 1);
+}
+
+// the points of cell c
+template <typename F>
+__device__ __forceinline__ void for_cell(const DTArgs &A, int c, F f) {
+  for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) f(A.sorted[i]);
+}
+
+// exhaustive gift-wrap query on face (p, a, b), 3D
+__device__ int gq3(const DTArgs &A, const GridParams &g, int ip, int ia, int ib,
+                   int lane, int &ovf) {
+  Face3 F;
+  F.ip = ip;
+  F.ia = ia;
+  F.ib = ib;
+  load_pt<3>(A.P, ip, F.p);
+  load_pt<3>(A.P, ia, F.a);
+  load_pt<3>(A.P, ib, F.b);
+  for (int k = 0; k < 3; ++k) {
+    F.V[k] = F.a[k] - F.p[k];
+    F.U[k] = F.b[k] - F.p[k];
+  }
+  F.n[0] = F.V[1] * F.U[2] - F.V[2] * F.U[1];
+  F.n[1] = F.V[2] * F.U[0] - F.V[0] * F.U[2];
+  F.n[2] = F.V[0] * F.U[1] - F.V[1] * F.U[0];
+  int best = -1;
+  float bx[3];
+  int cc[3];
+  for (int k = 0; k < 3; ++k)
+    cc[k] = cell_coord(g, (F.p[k] + F.a[k] + F.b[k]) * (1.f / 3.f), k);
+  if (lane < 27) {
+    int x = cc[0] + lane % 3 - 1, y = cc[1] + (lane / 3) % 3 - 1,
+        z = cc[2] + lane / 9 - 1;
+    if (x >= 0 && y >= 0 && z >= 0 && x < g.dims[0] && y < g.dims[1] && z < g.dims[2])
+      for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
+               [&](int j) { consider3(A, F, j, best, bx, ovf); });
+  }
+  best = tourney3(A, F, best, ovf);
+  // search region
+  bool full = true;
+  double cen[3] = {0, 0, 0}, rad = 0;
+  if (best >= 0) {
+    load_pt<3>(A.P, best, bx);
+    double a[3], b[3], c[3];
+    for (int k = 0; k < 3; ++k) {
+      a[k] = (double)F.a[k] - F.p[k];
+      b[k] = (double)F.b[k] - F.p[k];
+      c[k] = (double)bx[k] - F.p[k];
+    }
+    double bc[3] = {b[1] * c[2] - b[2] * c[1], b[2] * c[0] - b[0] * c[2],
+                    b[0] * c[1] - b[1] * c[0]};
+    double ca[3] = {c[1] * a[2] - c[2] * a[1], c[2] * a[0] - c[0] * a[2],
+                    c[0] * a[1] - c[1] * a[0]};
+    double ab[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                    a[0] * b[1] - a[1] * b[0]};
+    double det = a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2];
+    double perm = fabs(a[0]) * (fabs(b[1] * c[2]) + fabs(b[2] * c[1])) +
+                  fabs(a[1]) * (fabs(b[2] * c[0]) + fabs(b[0] * c[2])) +
+                  fabs(a[2]) * (fabs(b[0] * c[1]) + fabs(b[1] * c[0]));
+    if (fabs(det) > 1e-9 * perm) {
+      double la = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+      double lb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+      double lc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+      for (int k = 0; k < 3; ++k) cen[k] = (la * bc[k] + lb * ca[k] + lc * ab[k]) / (2 * det);
+      rad = sqrt(cen[0] * cen[0] + cen[1] * cen[1] + cen[2] * cen[2]);
+      for (int k = 0; k < 3; ++k) cen[k] += F.p[k];
+      rad = rad * (1 + 1e-6) + 1e-7 * (fabs(cen[0]) + fabs(cen[1]) + fabs(cen[2]));
+      full = false;
+    }
+  }
+  if (!full) {
+    int lo[3], hi[3];
+    int64_t ncell = 1;
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = max(0, (int)floor((cen[k] - rad - g.lo[k]) * g.inv_cs) - 1);
+      hi[k] = min(g.dims[k] - 1, (int)floor((cen[k] + rad - g.lo[k]) * g.inv_cs) + 1);
+      ncell *= (hi[k] - lo[k] + 1);
+    }
+    float r2 = (float)(rad * rad) * 1.0001f;
+    if (ncell <= 4096) {
+      int sx = hi[0] - lo[0] + 1, sy = hi[1] - lo[1] + 1;
+      for (int t = lane; t < ncell; t += 32) {
+        int x = lo[0] + t % sx, y = lo[1] + (t / sx) % sy, z = lo[2] + t / (sx * sy);
+        if (in_local(cc, x, y, z, 3)) continue;
+        // cell box vs sphere
+        float dd = 0.f;
+        int ci[3] = {x, y, z};
+        for (int k = 0; k < 3; ++k) {
+          float b0 = g.lo[k] + ci[k] * g.cs, b1 = b0 + g.cs;
+          float c = (float)cen[k];
+          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
+          dd += e * e;
+        }
+        if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
+        for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
+                 [&](int j) { consider3(A, F, j, best, bx, ovf); });
+      }
+    } else {
+      int blo[3], bhi[3];
+      int64_t nb = 1;
+      for (int k = 0; k < 3; ++k) {
+        blo[k] = lo[k] / g.bs;
+        bhi[k] = hi[k] / g.bs;
+        nb *= (bhi[k] - blo[k] + 1);
+      }
+      int sx = bhi[0] - blo[0] + 1, sy = bhi[1] - blo[1] + 1;
+      for (int64_t t = lane; t < nb; t += 32) {
+        int bxi = blo[0] + (int)(t % sx), byi = blo[1] + (int)((t / sx) % sy),
+            bzi = blo[2] + (int)(t / (sx * sy));
+        int bid = bxi + g.bdims[0] * (byi + g.bdims[1] * bzi);
+        if (A.blk_cnt[bid] == 0) continue;
+        float dd = 0.f;
+        for (int k = 0; k < 3; ++k) {
+          float b0 = A.blk_box[6 * bid + k], b1 = A.blk_box[6 * bid + 3 + k];
+          float c = (float)cen[k];
+          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
+          dd += e * e;
+        }
+        if (dd > r2 * 1.0001f + 1e-6f * g.cs * g.cs) continue;
+        for (int z = bzi * g.bs; z < min(bzi * g.bs + g.bs, g.dims[2]); ++z)
+          for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
+            for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
+              if (in_local(cc, x, y, z, 3)) continue;
+              for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
+                       [&](int j) { consider3(A, F, j, best, bx, ovf); });
+            }
+      }
+    }
+  } else {
+    // every block that may hold a point on the positive side
+    float nrm = sqrtf(F.n[0] * F.n[0] + F.n[1] * F.n[1] + F.n[2] * F.n[2]);
+    for (int bid = lane; bid < g.nblocks; bid += 32) {
+      if (A.blk_cnt[bid] == 0) continue;
+      float mx = -FLT_MAX, scale = 0.f;
+      for (int corner = 0; corner < 8; ++corner) {
+        float d = 0.f;
+        for (int k = 0; k < 3; ++k) {
+          float v = A.blk_box[6 * bid + ((corner >> k) & 1) * 3 + k] - F.p[k];
+          d += v * F.n[k];
+          scale = fmaxf(scale, fabsf(v));
+        }
+        mx = fmaxf(mx, d);
+      }
+      if (mx < -1e-4f * nrm * scale) continue;
+      int bxi = bid % g.bdims[0], byi = (bid / g.bdims[0]) % g.bdims[1],
+          bzi = bid / (g.bdims[0] * g.bdims[1]);
+      for (int z = bzi * g.bs; z < min(bzi * g.bs + g.bs, g.dims[2]); ++z)
+        for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
+          for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
+            if (in_local(cc, x, y, z, 3)) continue;
+            for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
+                     [&](int j) { consider3(A, F, j, best, bx, ovf); });
+          }
+    }
+  }
+  return tourney3(A, F, best, ovf);
+}
+
+// ---- 2D exhaustive query across edge (p, x): sgn=+1 triangles (p,x,y),
+// sgn=-1 triangles (p,y,x)
+struct Edge2 {
+  int ip, ix, sgn;
+  float p[2], x[2];
+  float X[2];
+};
+
+__device__ __forceinline__ int side2(const Edge2 &E, const float *y) {
+  float Y[2] = {y[0] - E.p[0], y[1] - E.p[1]};
+  int s = dmp::orient2_rel_filter<float>(E.X[0], E.X[1], Y[0], Y[1], 8.0f * DMP_U32);
+  if (!s) s = dmp::orient2_slow(E.p, E.x, y);
+  return s * E.sgn;
+}
+
+__device__ __forceinline__ int cmp2(const Edge2 &E, const float *bx,
+                                    const float *y, int &ovf) {
+  // <0 when y lies inside the circle of the current triangle
+  return E.sgn > 0 ? incirc2_sos(E.p, E.x, bx, y, &ovf)
+                   : incirc2_sos(E.p, bx, E.x, y, &ovf);
+}
+
+__device__ __forceinline__ void consider2(const DTArgs &A, const Edge2 &E, int j,
+                                          int &best, float *bx, int &ovf) {
+  if (j == E.ip || j == E.ix || A.dup[j]) return;
+  float y[2];
+  load_pt<2>(A.P, j, y);
+  if (side2(E, y) <= 0) return;
+  if (best < 0 || cmp2(E, bx, y, ovf) < 0) {
+    best = j;
+    bx[0] = y[0];
+    bx[1] = y[1];
+  }
+}
+
+__device__ __forceinline__ int tourney2(const DTArgs &A, const Edge2 &E,
+                                        int best, int &ovf) {
+  for (int o = 16; o; o >>= 1) {
+    int other = __shfl_xor_sync(0xffffffffu, best, o);
+    if (other >= 0 && other != best) {
+      if (best < 0) {
+        best = other;
+      } else {
+        float bx[2], ox[2];
+        load_pt<2>(A.P, best, bx);
+        load_pt<2>(A.P, other, ox);
+        if (cmp2(E, bx, ox, ovf) < 0) best = other;
+      }
+    }
+  }
+  return best;
+}
+
+__device__ int gq2(const DTArgs &A, const GridParams &g, int ip, int ix, int sgn,
+                   int lane, int &ovf) {
+  Edge2 E;
+  E.ip = ip;
+  E.ix = ix;
+  E.sgn = sgn;
+  load_pt<2>(A.P, ip, E.p);
+  load_pt<2>(A.P, ix, E.x);
+  E.X[0] = E.x[0] - E.p[0];
+  E.X[1] = E.x[1] - E.p[1];
+  int best = -1;
+  float bx[2];
+  int cc[3] = {cell_coord(g, 0.5f * (E.p[0] + E.x[0]), 0),
+               cell_coord(g, 0.5f * (E.p[1] + E.x[1]), 1), 0};
+  if (lane < 9) {
+    int x = cc[0] + lane % 3 - 1, y = cc[1] + lane / 3 - 1;
+    if (x >= 0 && y >= 0 && x < g.dims[0] && y < g.dims[1])
+      for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+  }
+  best = tourney2(A, E, best, ovf);
+  bool full = true;
+  double cen[2] = {0, 0}, rad = 0;
+  if (best >= 0) {
+    load_pt<2>(A.P, best, bx);
+    double a[2] = {(double)E.x[0] - E.p[0], (double)E.x[1] - E.p[1]};
+    double b[2] = {(double)bx[0] - E.p[0], (double)bx[1] - E.p[1]};
+    double det = a[0] * b[1] - a[1] * b[0];
+    double perm = fabs(a[0] * b[1]) + fabs(a[1] * b[0]);
+    if (fabs(det) > 1e-9 * perm) {
+      double la = a[0] * a[0] + a[1] * a[1], lb = b[0] * b[0] + b[1] * b[1];
+      cen[0] = (b[1] * la - a[1] * lb) / (2 * det);
+      cen[1] = (a[0] * lb - b[0] * la) / (2 * det);
+      rad = sqrt(cen[0] * cen[0] + cen[1] * cen[1]);
+      cen[0] += E.p[0];
+      cen[1] += E.p[1];
+      rad = rad * (1 + 1e-6) + 1e-7 * (fabs(cen[0]) + fabs(cen[1]));
+      full = false;
+    }
+  }
+  if (!full) {
+    int lo[2], hi[2];
+    int64_t ncell = 1;
+    for (int k = 0; k < 2; ++k) {
+      lo[k] = max(0, (int)floor((cen[k] - rad - g.lo[k]) * g.inv_cs) - 1);
+      hi[k] = min(g.dims[k] - 1, (int)floor((cen[k] + rad - g.lo[k]) * g.inv_cs) + 1);
+      ncell *= (hi[k] - lo[k] + 1);
+    }
+    float r2 = (float)(rad * rad) * 1.0001f;
+    if (ncell <= 4096) {
+      int sx = hi[0] - lo[0] + 1;
+      for (int t = lane; t < ncell; t += 32) {
+        int x = lo[0] + t % sx, y = lo[1] + t / sx;
+        if (in_local(cc, x, y, 0, 2)) continue;
+        float dd = 0.f;
+        int ci[2] = {x, y};
+        for (int k = 0; k < 2; ++k) {
+          float b0 = g.lo[k] + ci[k] * g.cs, b1 = b0 + g.cs;
+          float c = (float)cen[k];
+          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
+          dd += e * e;
+        }
+        if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
+        for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+      }
+    } else {
+      int blo[2] = {lo[0] / g.bs, lo[1] / g.bs}, bhi[2] = {hi[0] / g.bs, hi[1] / g.bs};
+      int sx = bhi[0] - blo[0] + 1;
+      int64_t nb = (int64_t)sx * (bhi[1] - blo[1] + 1);
+      for (int64_t t = lane; t < nb; t += 32) {
+        int bxi = blo[0] + (int)(t % sx), byi = blo[1] + (int)(t / sx);
+        int bid = bxi + g.bdims[0] * byi;
+        if (A.blk_cnt[bid] == 0) continue;
+        float dd = 0.f;
+        for (int k = 0; k < 2; ++k) {
+          float b0 = A.blk_box[6 * bid + k], b1 = A.blk_box[6 * bid + 3 + k];
+          float c = (float)cen[k];
+          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
+          dd += e * e;
+        }
+        if (dd > r2 * 1.0001f + 1e-6f * g.cs * g.cs) continue;
+        for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
+          for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
+            if (in_local(cc, x, y, 0, 2)) continue;
+            for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+          }
+      }
+    }
+  } else {
+    float nrm = sqrtf(E.X[0] * E.X[0] + E.X[1] * E.X[1]);
+    float n0 = -E.X[1] * sgn, n1 = E.X[0] * sgn;
+    for (int bid = lane; bid < g.nblocks; bid += 32) {
+      if (A.blk_cnt[bid] == 0) continue;
+      float mx = -FLT_MAX, scale = 0.f;
+      for (int corner = 0; corner < 4; ++corner) {
+        float v0 = A.blk_box[6 * bid + (corner & 1) * 3 + 0] - E.p[0];
+        float v1 = A.blk_box[6 * bid + ((corner >> 1) & 1) * 3 + 1] - E.p[1];
+        mx = fmaxf(mx, v0 * n0 + v1 * n1);
+        scale = fmaxf(scale, fmaxf(fabsf(v0), fabsf(v1)));
+      }
+      if (mx < -1e-4f * nrm * scale) continue;
+      int bxi = bid % g.bdims[0], byi = bid / g.bdims[0];
+      for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
+        for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
+          if (in_local(cc, x, y, 0, 2)) continue;
+          for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+        }
+    }
+  }
+  return tourney2(A, E, best, ovf);
+}
+
+__device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane) {
+  int hit = -1;
+  for (int k = lane; k < S.nopen; k += 32) {
+    int3 e = S.open[k];
+    if (e.x == t && e.y == s) hit = k;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, hit >= 0);
+  if (!m) return -1;
+  return __shfl_sync(0xffffffffu, hit, __ffs(m) - 1);
+}
+
+__global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
+  __shared__ WarpL2 sm[L2_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpL2 &S = sm[w];
+  const GridParams g = *A.gp;
+  const int64_t nesc = A.counters[DM_CNT_ESCALATED];
+  for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
+       k += (int64_t)gridDim.x * L2_WARPS) {
+    int4 sd = A.esc_seed[k];
+    const int ip = sd.x & ~(1 << 30);
+    const bool certified = (sd.x >> 30) & 1;
+    int ovf = 0;
+    int3 seed = make_int3(-1, -1, -1);
+    if (certified) {
+      seed = make_int3(sd.y, sd.z, sd.w);
+    } else if (sd.w >= 0) {
+      int f[3][2] = {{sd.y, sd.z}, {sd.z, sd.w}, {sd.w, sd.y}};
+      for (int t = 0; t < 3 && seed.x < 0; ++t) {
+        int a = f[t][0], b = f[t][1];
+        int xp = gq3(A, g, ip, a, b, lane, ovf);
+        int xm = gq3(A, g, ip, b, a, lane, ovf);
+        if (xp < 0 && xm < 0) continue;
+        bool ok = true;
+        if (xp >= 0 && xm >= 0) {
+          float pr[3], ar[3], br[3], xr[3], mr[3];
+          load_pt<3>(A.P, ip, pr);
+          load_pt<3>(A.P, a, ar);
+          load_pt<3>(A.P, b, br);
+          load_pt<3>(A.P, xp, xr);
+          load_pt<3>(A.P, xm, mr);
+          ok = insph3_sos(pr, ar, br, xr, mr, &ovf) > 0;
+        }
+        if (ok) seed = xp >= 0 ? make_int3(a, b, xp) : make_int3(b, a, xm);
+      }
+    }
+    if (seed.x < 0) {
+      if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
+      continue;
+    }
+    if (lane == 0) {
+      S.ntri = 1;
+      S.tri[0] = seed;
+      S.open[0] = make_int3(seed.x, seed.y, seed.z);
+      S.open[1] = make_int3(seed.y, seed.z, seed.x);
+      S.open[2] = make_int3(seed.z, seed.x, seed.y);
+      S.nopen = 3;
+      S.flags = 0;
+    }
+    __syncwarp();
+    while (S.nopen > 0) {
+      int3 e = S.open[S.nopen - 1];
+      __syncwarp();
+      if (lane == 0) S.nopen--;
+      __syncwarp();
+      int u = e.x, v = e.y;
+      int y = gq3(A, g, ip, v, u, lane, ovf);
+      if (y < 0) continue;  // convex-hull face
+      if (S.ntri >= L2_MAXTRI) {
+        if (lane == 0) S.flags |= 1;
+        __syncwarp();
+        break;
+      }
+      if (lane == 0) S.tri[S.ntri++] = make_int3(v, u, y);
+      __syncwarp();
+      int es[2][3] = {{u, y, v}, {y, v, u}};
+      for (int q = 0; q < 2; ++q) {
+        int r = find_rev2(S, es[q][0], es[q][1], lane);
+        if (lane == 0) {
+          if (r >= 0) {
+            S.open[r] = S.open[S.nopen - 1];
+            S.nopen--;
+          } else if (S.nopen < L2_MAXOPEN) {
+            S.open[S.nopen++] = make_int3(es[q][0], es[q][1], es[q][2]);
+          } else {
+            S.flags |= 1;
+          }
+        }
+        __syncwarp();
+      }
+      if (S.flags) break;
+    }
+    if (S.flags && lane == 0) flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    for (int t0 = 0; t0 < S.ntri; t0 += 32) {
+      int t = t0 + lane;
+      bool own = false;
+      int3 tr = make_int3(0, 0, 0);
+      if (t < S.ntri) {
+        tr = S.tri[t];
+        own = ip < tr.x && ip < tr.y && ip < tr.z;
+      }
+      int64_t q = warp_append(&A.counters[DM_CNT_CELLS], own);
+      if (own) {
+        if (q < A.cap_cells_out) {
+          reinterpret_cast<int4 *>(A.cells)[q] = make_int4(ip, tr.x, tr.y, tr.z);
+        } else {
+          flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
+  __shared__ WarpL2 sm[L2_WARPS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpL2 &S = sm[w];
+  const GridParams g = *A.gp;
+  const int64_t nesc = A.counters[DM_CNT_ESCALATED];
+  for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
+       k += (int64_t)gridDim.x * L2_WARPS) {
+    int4 sd = A.esc_seed[k];
+    const int ip = sd.x & ~(1 << 30);
+    const bool certified = (sd.x >> 30) & 1;
+    int ovf = 0;
+    int a = -1, b = -1;
+    if (certified) {
+      a = sd.y;
+      b = sd.z;
+    } else {
+      // nearest-point edge candidates from the level-1 record, else exhaustive
+      int cand[2] = {sd.y, sd.z};
+      for (int t = 0; t < 2 && a < 0; ++t) {
+        int q1 = cand[t];
+        if (q1 < 0) continue;
+        int xp = gq2(A, g, ip, q1, +1, lane, ovf);
+        int xm = gq2(A, g, ip, q1, -1, lane, ovf);
+        if (xp < 0 && xm < 0) continue;
+        bool ok = true;
+        if (xp >= 0 && xm >= 0) {
+          float pr[2], qr[2], xr[2], mr[2];
+          load_pt<2>(A.P, ip, pr);
+          load_pt<2>(A.P, q1, qr);
+          load_pt<2>(A.P, xp, xr);
+          load_pt<2>(A.P, xm, mr);
+          ok = incirc2_sos(pr, qr, xr, mr, &ovf) > 0;
+        }
+        if (ok) {
+          if (xp >= 0) {
+            a = q1;
+            b = xp;
+          } else {
+            a = xm;
+            b = q1;
+          }
+        }
+      }
+    }
+    if (a < 0) {
+      if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
+      continue;
+    }
+    if (lane == 0) {
+      S.ntri = 1;
+      S.tri[0] = make_int3(a, b, 0);
+      S.flags = 0;
+    }
+    __syncwarp();
+    bool hull = false;
+    int cur = b;
+    while (true) {
+      int nx = gq2(A, g, ip, cur, +1, lane, ovf);
+      if (nx < 0) {
+        hull = true;
+        break;
+      }
+      if (nx == a) break;
+      if (S.ntri >= L2_MAXTRI) {
+        if (lane == 0) S.flags |= 1;
+        __syncwarp();
+        break;
+      }
+      if (lane == 0) S.tri[S.ntri++] = make_int3(cur, nx, 0);
+      __syncwarp();
+      cur = nx;
+    }
+    if (hull && !S.flags) {
+      cur = a;
+      while (true) {
+        int pv = gq2(A, g, ip, cur, -1, lane, ovf);
+        if (pv < 0) break;
+        if (S.ntri >= L2_MAXTRI) {
+          if (lane == 0) S.flags |= 1;
+          __syncwarp();
+          break;
+        }
+        if (lane == 0) S.tri[S.ntri++] = make_int3(pv, cur, 0);
+        __syncwarp();
+        cur = pv;
+      }
+    }
+    if (S.flags && lane == 0) flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    for (int t0 = 0; t0 < S.ntri; t0 += 32) {
+      int t = t0 + lane;
+      bool own = false;
+      int3 tr = make_int3(0, 0, 0);
+      if (t < S.ntri) {
+        tr = S.tri[t];
+        own = ip < tr.x && ip < tr.y;
+      }
+      int64_t q = warp_append(&A.counters[DM_CNT_CELLS], own);
+      if (own) {
+        if (q < A.cap_cells_out) {
+          A.cells[3 * q] = ip;
+          A.cells[3 * q + 1] = tr.x;
+          A.cells[3 * q + 2] = tr.y;
+        } else {
+          flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+int delaunay_workspace(int dim, int64_t n, size_t *bytes) {
+  Carve c(nullptr, 0);
+  DTArgs a;
+  *bytes = carve_dt(c, a, dim, n) + 256;
+  return DM_OK;
+}
+
+int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
+             int64_t cap_cells, int64_t *counters, void *ws, size_t ws_bytes,
+             cudaStream_t s) {
+  DM_ARG_CHECK(dim == 2 || dim == 3, "dim must be 2 or 3");
+  DM_ARG_CHECK(n >= 0 && n < (1 << 30), "n out of range");
+  DM_ARG_CHECK(pts != nullptr || n == 0, "points is null");
+  DM_ARG_CHECK(cells != nullptr && counters != nullptr, "null output");
+  DM_ARG_CHECK(((uintptr_t)pts & (dim == 3 ? 15 : 7)) == 0, "points misaligned");
+  DM_ARG_CHECK(((uintptr_t)cells & 15) == 0, "cells misaligned");
+  Carve c(ws, ws_bytes);
+  DTArgs a;
+  carve_dt(c, a, dim, n);
+  if (!c.ok() || ws == nullptr) {
+    set_error("delaunay: workspace %zu < required %zu", ws_bytes, c.used);
+    return DM_ERR_WORKSPACE;
+  }
+  a.dim = dim;
+  a.n = n;
+  a.P = pts;
+  a.cells = cells;
+  a.cap_cells_out = cap_cells;
+  a.counters = counters;
+  DM_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int64_t) * DM_NCOUNTERS, s));
+  if (n == 0) return DM_OK;
+  DM_CUDA_TRY(cudaMemsetAsync(a.cell_cnt, 0, sizeof(int32_t) * a.cap_cells, s));
+  int nb = grid_for(n, 256);
+  k_bbox_init<<<1, 32, 0, s>>>(a.bbox);
+  if (dim == 3)
+    k_bbox<3><<<nb, 256, 0, s>>>(pts, n, a.bbox, counters);
+  else
+    k_bbox<2><<<nb, 256, 0, s>>>(pts, n, a.bbox, counters);
+  k_grid_params<<<1, 32, 0, s>>>(a.gp, a.bbox, n, dim, a.cap_cells, a.cap_blocks);
+  if (dim == 3)
+    k_cell_count<3><<<nb, 256, 0, s>>>(pts, n, a.gp, a.cell_of, a.slot, a.cell_cnt);
+  else
+    k_cell_count<2><<<nb, 256, 0, s>>>(pts, n, a.gp, a.cell_of, a.slot, a.cell_cnt);
+  DM_LAUNCH_CHECK();
+  int rc = exclusive_scan_i32(a.cell_cnt, a.cell_start, a.cap_cells, a.scan_tmp, s);
+  if (rc) return rc;
+  k_cell_scatter<<<nb, 256, 0, s>>>(n, a.cell_of, a.slot, a.cell_start, a.sorted);
+  int ncb = grid_for(a.cap_cells, 256);
+  if (dim == 3) {
+    k_cell_sort<3><<<ncb, 256, 0, s>>>(pts, a.gp, a.cell_start, a.sorted, a.dup, counters);
+    k_block_boxes<3><<<grid_for(a.cap_blocks, 128), 128, 0, s>>>(
+        pts, a.gp, a.cell_start, a.sorted, a.blk_cnt, a.blk_box);
+  } else {
+    k_cell_sort<2><<<ncb, 256, 0, s>>>(pts, a.gp, a.cell_start, a.sorted, a.dup, counters);
+    k_block_boxes<2><<<grid_for(a.cap_blocks, 128), 128, 0, s>>>(
+        pts, a.gp, a.cell_start, a.sorted, a.blk_cnt, a.blk_box);
+  }
+  DM_LAUNCH_CHECK();
+  // (non-finite coordinates are reported through DM_FLAG_NONFINITE; the star
+  // kernels still run on the single-cell grid and stay bounded)
+  int64_t nwb = (n + L1_WARPS - 1) / L1_WARPS;
+  int g1 = (int)std::min<int64_t>(nwb, (int64_t)kSMs * 16);
+  if (dim == 3)
+    k_star3_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
+  else
+    k_star2_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
+  DM_LAUNCH_CHECK();
+  int g2 = kSMs * 8;
+  if (dim == 3)
+    k_star3_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
+  else
+    k_star2_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+}  // namespace dm

@@ -1,0 +1,321 @@
+// Gradient limiting of mesh-size grids and the drop-in unique_edges.
+#include "dm_common.cuh"
+
+namespace dm {
+
+// ---------------------------------------------------------------------------
+// limgrad.  The reference (sizing/cpp/FastHJ.cpp:63-157) relaxes
+//   f_i <- min(f_i, f_j + elen * dfdx)
+// over the 6-neighbour stencil of a column-major grid with an active set
+// until no value drops by more than ftol = min(f) * sqrt(eps).  Its fixed
+// point is the min-plus distance transform f_i = min_k f_k + c |i - k|_1
+// (c = elen * dfdx, grid steps counted in L1), which is separable by axis.
+// Each axis is one forward and one backward sweep per grid line; the result
+// is that fixed point exactly (the reference stops within ftol of it).
+__global__ void k_limgrad_axis(double *f, int d0, int d1, int d2, int axis,
+                               double c) {
+  int64_t nlines, len, stride;
+  if (axis == 0) {
+    nlines = (int64_t)d1 * d2;
+    len = d0;
+    stride = 1;
+  } else if (axis == 1) {
+    nlines = (int64_t)d0 * d2;
+    len = d1;
+    stride = d0;
+  } else {
+    nlines = (int64_t)d0 * d1;
+    len = d2;
+    stride = (int64_t)d0 * d1;
+  }
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nlines;
+       l += (int64_t)gridDim.x * blockDim.x) {
+    int64_t base;
+    if (axis == 0)
+      base = l * d0;
+    else if (axis == 1)
+      base = (l % d0) + (l / d0) * (int64_t)d0 * d1;
+    else
+      base = l;
+    double prev = f[base];
+    for (int64_t i = 1; i < len; ++i) {
+      double *q = f + base + i * stride;
+      double v = fmin(*q, prev + c);
+      *q = v;
+      prev = v;
+    }
+    prev = f[base + (len - 1) * stride];
+    for (int64_t i = len - 2; i >= 0; --i) {
+      double *q = f + base + i * stride;
+      double v = fmin(*q, prev + c);
+      *q = v;
+      prev = v;
+    }
+  }
+}
+
+int limgrad(const int32_t *dims, double elen, double dfdx, int imax, double *f,
+            cudaStream_t s) {
+  DM_ARG_CHECK(dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0, "dims");
+  DM_ARG_CHECK(imax >= 0, "imax");
+  double c = elen * dfdx;
+  for (int axis = 0; axis < 3; ++axis) {
+    int64_t nl = axis == 0 ? (int64_t)dims[1] * dims[2]
+                           : axis == 1 ? (int64_t)dims[0] * dims[2]
+                                       : (int64_t)dims[0] * dims[1];
+    if ((axis == 0 ? dims[0] : axis == 1 ? dims[1] : dims[2]) < 2) continue;
+    k_limgrad_axis<<<grid_for(nl, 128), 128, 0, s>>>(f, dims[0], dims[1], dims[2],
+                                                     axis, c);
+  }
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// unique_edges (geometry/cpp/fast_geometry.cpp:30-77): (min, max) pairs,
+// sorted lexicographically, duplicates removed.  Counting sort by the first
+// key, then each bucket is sorted and deduplicated on the second key.
+__global__ void k_ue_count(const int32_t *e, int64_t m, int32_t *cnt,
+                           int32_t *key, int32_t *slot) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int a = e[2 * i], b = e[2 * i + 1];
+    int lo = min(a, b);
+    key[i] = lo;
+    slot[i] = atomicAdd(&cnt[lo], 1);
+  }
+}
+
+__global__ void k_ue_scatter(const int32_t *e, int64_t m, const int32_t *start,
+                             const int32_t *key, const int32_t *slot,
+                             int32_t *val) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int a = e[2 * i], b = e[2 * i + 1];
+    val[start[key[i]] + slot[i]] = max(a, b);
+  }
+}
+
+// per bucket: insertion sort + unique in place, ucnt[v] = unique count
+__global__ void k_ue_sort(int64_t n, const int32_t *start, int32_t *val,
+                          int32_t *ucnt) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    int b = start[v], e = start[v + 1];
+    for (int i = b + 1; i < e; ++i) {
+      int x = val[i], j = i - 1;
+      while (j >= b && val[j] > x) {
+        val[j + 1] = val[j];
+        --j;
+      }
+      val[j + 1] = x;
+    }
+    int u = 0;
+    for (int i = b; i < e; ++i)
+      if (i == b || val[i] != val[i - 1]) val[b + u++] = val[i];
+    ucnt[v] = u;
+  }
+}
+
+__global__ void k_ue_write(int64_t n, const int32_t *start, const int32_t *val,
+                           const int32_t *ustart, int32_t *out) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    int b = start[v], o = ustart[v], u = ustart[v + 1] - o;
+    for (int i = 0; i < u; ++i) {
+      out[2 * (o + i)] = (int32_t)v;
+      out[2 * (o + i) + 1] = val[b + i];
+    }
+  }
+}
+
+static size_t carve_ue(Carve &c, int64_t n, int64_t m, int32_t **cnt,
+                       int32_t **start, int32_t **key, int32_t **slot,
+                       int32_t **val, int32_t **ucnt, int32_t **ustart,
+                       int32_t **tmp) {
+  *cnt = c.take<int32_t>(n);
+  *start = c.take<int32_t>(n + 1);
+  *key = c.take<int32_t>(m);
+  *slot = c.take<int32_t>(m);
+  *val = c.take<int32_t>(m);
+  *ucnt = c.take<int32_t>(n);
+  *ustart = c.take<int32_t>(n + 1);
+  *tmp = c.take<int32_t>(scan_tmp_elems(n));
+  return c.used;
+}
+
+int unique_edges_workspace(int64_t n, int64_t m, size_t *bytes) {
+  Carve c(nullptr, 0);
+  int32_t *a, *b, *d, *e, *f, *g, *h, *t;
+  *bytes = carve_ue(c, n, m, &a, &b, &d, &e, &f, &g, &h, &t) + 256;
+  return DM_OK;
+}
+
+int unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
+                 int64_t *n_out, void *ws, size_t ws_bytes, cudaStream_t s) {
+  DM_ARG_CHECK(n >= 0 && m >= 0, "sizes");
+  DM_ARG_CHECK(n_out != nullptr, "n_out");
+  Carve c(ws, ws_bytes);
+  int32_t *cnt, *start, *key, *slot, *val, *ucnt, *ustart, *tmp;
+  carve_ue(c, n, m, &cnt, &start, &key, &slot, &val, &ucnt, &ustart, &tmp);
+  if (!c.ok() || !ws) {
+    set_error("unique_edges: workspace %zu < required %zu", ws_bytes, c.used);
+    return DM_ERR_WORKSPACE;
+  }
+  *n_out = 0;
+  if (m == 0 || n == 0) return DM_OK;
+  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
+  int nb = grid_for(m, 256);
+  k_ue_count<<<nb, 256, 0, s>>>(edges, m, cnt, key, slot);
+  int rc = exclusive_scan_i32(cnt, start, n, tmp, s);
+  if (rc) return rc;
+  k_ue_scatter<<<nb, 256, 0, s>>>(edges, m, start, key, slot, val);
+  k_ue_sort<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ucnt);
+  rc = exclusive_scan_i32(ucnt, ustart, n, tmp, s);
+  if (rc) return rc;
+  k_ue_write<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ustart, out);
+  DM_LAUNCH_CHECK();
+  int32_t total = 0;
+  DM_CUDA_TRY(cudaMemcpyAsync(&total, ustart + n, sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaStreamSynchronize(s));
+  *n_out = total;
+  return DM_OK;
+}
+
+}  // namespace dm
+
+namespace dm {
+
+// ---------------------------------------------------------------------------
+// Mesh size from a velocity grid (sizing/mesh_size_function.py:146-221):
+// unit scale, water replacement, wavelength / gradient sizing, [hmin, hmax]
+// clamp and the Courant bound, elementwise in FP64.
+struct SizeParams {
+  double scale;       // unit conversion factor applied to vp
+  double vp_water;    // replacement for vp < 1e-3 (if replace != 0)
+  int replace;
+  double wl, freq;    // wavelength sizing when wl > 0
+  double grad;        // gradient sizing when grad > 0 (uses gterm)
+  double hmin, hmax;
+  double dt, cr_max, space_order;
+  int dim;
+};
+
+__global__ void k_size_from_vp(double *vp, int64_t n, const double *gterm,
+                               SizeParams sp, double *cell) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = vp[i] * sp.scale;
+    if (sp.replace && v < 1e-3) v = sp.vp_water;
+    vp[i] = v;
+    double h = sp.hmin;
+    if (sp.wl > 0 || sp.grad > 0) {
+      double a = sp.wl > 0 ? v / (sp.freq * sp.wl) : 99999.0;
+      double b = sp.grad > 0 ? gterm[i] : 99999.0;
+      h = fmin(a, b);
+    }
+    if (h < sp.hmin) h = sp.hmin;
+    if (h > sp.hmax) h = sp.hmax;
+    if (sp.cr_max != 0.0 && sp.dt != 0.0 && sp.space_order != 0.0) {
+      double cr_old = (v * sp.dt) / (sp.dim * h);
+      double crm = sp.cr_max / (sp.dim * sp.space_order);
+      double dxn = (v * sp.dt) / (sp.dim * crm);
+      if (cr_old > crm) h = dxn;
+    }
+    cell[i] = h;
+  }
+}
+
+// flag: some vp < 1e-3 (after unit scaling) outside the first row (the
+// reference replaces water velocities only when such a cell exists,
+// sizing/mesh_size_function.py:154-165)
+__global__ void k_water_flag(const double *vp, int64_t n, int64_t row_len,
+                             double scale, int *flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (vp[i] * scale < 1e-3 && i >= row_len) *flag = 1;
+}
+
+int size_from_velocity(double *vp, int64_t n, int64_t row_len,
+                       const double *gterm, const SizeParams *sp_in,
+                       double *cell, int *replaced_host, void *ws,
+                       cudaStream_t s) {
+  SizeParams sp = *sp_in;
+  int *flag = (int *)ws;
+  DM_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
+  k_water_flag<<<grid_for(n, 256), 256, 0, s>>>(vp, n, row_len, sp.scale, flag);
+  int h = 0;
+  DM_CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaStreamSynchronize(s));
+  sp.replace = h;
+  if (h && (sp.vp_water < 1300 || sp.vp_water > 1800)) {
+    set_error("vp_water is None or out of bounds. It should be >1300 and <1800 m/s");
+    return DM_ERR_ARG;
+  }
+  if (replaced_host) *replaced_host = h;
+  k_size_from_vp<<<grid_for(n, 256), 256, 0, s>>>(vp, n, gterm, sp, cell);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// domain pad (sizing/mesh_size_function.py:526-587): pad a C-order grid by
+// pre[k] / post[k] cells per axis; mode 0 = edge, 1 = constant (value
+// cval), 2 = linear ramp to cval (numpy.pad semantics).
+struct PadArgs {
+  int n[3], pre[3], post[3];
+};
+
+__global__ void k_pad(const double *src, PadArgs a, int dim, int mode,
+                      double cval, double *dst) {
+  int m[3];
+  for (int k = 0; k < 3; ++k) m[k] = a.n[k] + a.pre[k] + a.post[k];
+  int64_t total = (int64_t)m[0] * m[1] * m[2];
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < total;
+       o += (int64_t)gridDim.x * blockDim.x) {
+    int idx[3] = {(int)(o / ((int64_t)m[1] * m[2])), (int)((o / m[2]) % m[1]),
+                  (int)(o % m[2])};
+    int sidx[3], c[3];
+    bool inside = true;
+    for (int k = 0; k < 3; ++k) {
+      sidx[k] = idx[k] - a.pre[k];
+      if (sidx[k] < 0 || sidx[k] >= a.n[k]) inside = false;
+      c[k] = min(max(sidx[k], 0), a.n[k] - 1);
+    }
+    double v = src[((int64_t)c[0] * a.n[1] + c[1]) * a.n[2] + c[2]];
+    if (!inside && mode == 1) {
+      v = cval;
+    } else if (!inside && mode == 2) {
+      // numpy.pad linear_ramp, applied axis by axis: the outermost pad cell
+      // equals cval, the ramp is linear in the distance to the edge.
+      for (int k = 0; k < dim; ++k) {
+        int i = sidx[k];
+        if (i < 0)
+          v = v + (cval - v) * ((double)(-i) / a.pre[k]);
+        else if (i >= a.n[k])
+          v = v + (cval - v) * ((double)(i - a.n[k] + 1) / a.post[k]);
+      }
+    }
+    dst[o] = v;
+  }
+}
+
+int pad_grid(const double *src, const int *n, const int *pre, const int *post,
+             int dim, int mode, double cval, double *dst, cudaStream_t s) {
+  DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
+  DM_ARG_CHECK(mode >= 0 && mode <= 2, "mode");
+  PadArgs a;
+  int64_t total = 1;
+  for (int k = 0; k < 3; ++k) {
+    a.n[k] = k < dim ? n[k] : 1;
+    a.pre[k] = k < dim ? pre[k] : 0;
+    a.post[k] = k < dim ? post[k] : 0;
+    total *= (int64_t)(a.n[k] + a.pre[k] + a.post[k]);
+  }
+  k_pad<<<grid_for(total, 256), 256, 0, s>>>(src, a, dim, mode, cval, dst);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+}  // namespace dm

@@ -1,0 +1,331 @@
+"""Mesh size functions from seismic velocity models, built on the GPU.
+
+Drop-in for sizing/mesh_size_function.py of the reference:
+get_sizing_function_from_segy (34-239) with the same keyword options and
+defaults, read_velocity_model (590-606) and its binary / SEG-Y readers.
+The size grid is computed by dm_size_from_velocity (wavelength sizing,
+clamp, Courant bound), dm_limgrad (gradation limiting) and dm_pad_grid
+(domain pad); the resulting SizeFunction evaluates with dm_sizing_eval
+(linear, extrapolating interpolation like RegularGridInterpolator with
+bounds_error=False, fill_value=None).
+"""
+import warnings
+
+import numpy as np
+import torch
+
+from .. import _device as D
+from .. import _native as N
+from .size_function import SizeFunction
+
+__all__ = [
+    "get_sizing_function_from_segy",
+    "write_velocity_model",
+    "plot_sizing_function",
+    "read_velocity_model",
+    "GridSizing",
+]
+
+
+class GridSizing:
+    """Device-resident size grid with linear interpolation on the GPU.
+
+    ``values`` (n0, n1[, n2]) on axes linspace(bbox[2k], bbox[2k+1], n_k);
+    query columns are in the same axis order as the grid.
+    """
+
+    device_grid = True
+
+    def __init__(self, values, bbox):
+        v = np.asarray(values)
+        self.dim = v.ndim
+        self.shape = v.shape
+        self.bbox = tuple(float(b) for b in bbox)
+        self.values = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float32)).to(D.device())
+        self.grid = np.asarray(values)
+
+    @classmethod
+    def from_device(cls, values_dev, bbox):
+        obj = cls.__new__(cls)
+        obj.dim = values_dev.dim()
+        obj.shape = tuple(values_dev.shape)
+        obj.bbox = tuple(float(b) for b in bbox)
+        obj.values = values_dev.float().contiguous()
+        obj.grid = None
+        return obj
+
+    def fill_struct(self, s):
+        s.kind = N.SIZING_GRID
+        s.dim = self.dim
+        s.grid = self.values.data_ptr()
+        for k in range(3):
+            s.n[k] = self.shape[k] if k < self.dim else 1
+            s.lo[k] = self.bbox[2 * k] if k < self.dim else 0.0
+            s.hi[k] = self.bbox[2 * k + 1] if k < self.dim else 1.0
+
+    def __call__(self, x):
+        if isinstance(x, tuple):
+            x = np.column_stack([np.ravel(c) for c in x])
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.float32).reshape(-1, self.dim))
+        n = x.shape[0]
+        s = N.Sizing()
+        self.fill_struct(s)
+        xd = torch.from_numpy(x).to(D.device())
+        h = D.empty((n,), torch.float32)
+        N.call("dm_sizing_eval", s, D.ptr(xd), n, self.dim, D.ptr(h), D.stream_ptr())
+        return h.double().cpu().numpy()
+
+
+def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
+    r"""Build a mesh size function from a seismic velocity model (same
+    keywords as the reference: velocity_data, vp_water, hmin, hmax, wl, freq,
+    grad, grade, stencil_size, space_order, dt, cr_max, pad_style,
+    domain_pad, units, nz, nx, ny, byte_order, axes_order, axes_order_sort,
+    dtype).  Returns a SizeFunction whose grid lives on the GPU."""
+    sz_opts = {
+        "velocity_data": None,
+        "vp_water": 1500.0,
+        "hmin": 150.0,
+        "hmax": 10000.0,
+        "wl": 0,
+        "freq": 2.0,
+        "grad": 0.0,
+        "grade": 0.0,
+        "stencil_size": 10.0,
+        "space_order": 1,
+        "dt": 0.0,
+        "cr_max": 1.0,
+        "pad_style": "edge",
+        "domain_pad": 0.0,
+        "units": "m-s",
+        "nz": None,
+        "nx": None,
+        "ny": None,
+        "byte_order": "byte_order",
+        "axes_order": (0, 1, 2),
+        "axes_order_sort": "F",
+        "dtype": "float32",
+    }
+    if comm is not None and getattr(comm, "size", 1) > 1:
+        raise NotImplementedError("the GPU engine builds sizing functions on one GPU")
+    sz_opts.update(kwargs)
+    vp = sz_opts["velocity_data"]
+    nz, nx, ny = sz_opts["nz"], sz_opts["nx"], sz_opts["ny"]
+    if vp is None:
+        vp, nz, nx, ny = read_velocity_model(
+            filename,
+            nz=nz,
+            nx=nx,
+            ny=ny,
+            byte_order=sz_opts["byte_order"],
+            axes_order=sz_opts["axes_order"],
+            axes_order_sort=sz_opts["axes_order_sort"],
+            dtype=sz_opts["dtype"],
+        )
+    scale = 1.0
+    if sz_opts["units"] == "km-s":
+        print("Converting from km-s to m-s...", flush=True)
+        scale = 1000.0
+    elif sz_opts["units"] == "ft-s":
+        print("Converting from ft-s to m-s...", flush=True)
+        scale = 0.30
+
+    if len(bbox) == 4:
+        dim = 2
+    elif len(bbox) == 6:
+        dim = 3
+    else:
+        raise ValueError("Dimension not supported")
+
+    allowed = {
+        "hmin", "hmax", "wl", "freq", "cr_max", "dt", "space_order", "grad", "grade",
+        "stencil_size", "pad_style", "domain_pad", "units", "nz", "nx", "ny",
+        "byte_order", "axes_order", "axes_order_sort", "dtype", "velocity_data", "vp_water",
+    }
+    for key in kwargs:
+        if key not in allowed:
+            raise ValueError("Option %s with parameter %s not recognized " % (key, kwargs[key]))
+
+    vp_host = np.ascontiguousarray(np.asarray(vp, dtype=np.float64))
+    shape = vp_host.shape
+    vpd = torch.from_numpy(vp_host).to(D.device())
+    cell = torch.empty_like(vpd)
+    if sz_opts["wl"] < 0:
+        raise ValueError("Parameter `wl` must be set > 0")
+    if sz_opts["freq"] < 0.0:
+        raise ValueError("Parameter `freq` must be set > 0.0")
+    if sz_opts["grad"] < 0:
+        raise ValueError("Parameter grad must be > 0")
+    if sz_opts["wl"] > 0:
+        print(
+            f"Mesh sizes will be built to resolve an estimate of wavelength of a "
+            f"{sz_opts['freq']}  hz wavelet with {sz_opts['wl']} vertices",
+            flush=True,
+        )
+    gterm = None
+    if sz_opts["grad"] > 0:
+        raise NotImplementedError("gradient-based sizing (grad > 0) has no device kernel yet")
+    if sz_opts["dt"] != 0.0 and sz_opts["cr_max"] != 0.0 and sz_opts["space_order"] != 0:
+        if sz_opts["cr_max"] < 0:
+            raise ValueError("Parameter `cr_max` must be > 0.0")
+        if sz_opts["dt"] < 0:
+            raise ValueError("Parameter `dt` must be > 0.0")
+        if sz_opts["space_order"] < 1:
+            raise ValueError("Parameter `space_order` must be >= 1 ")
+        print(f"Enforcing timestep of {sz_opts['dt']} seconds...", flush=True)
+    print(f"Enforcing minimum edge length of {sz_opts['hmin']}")
+    print(f"Enforcing maximum edge length of {sz_opts['hmax']}")
+    ws = D.workspace(256)
+    replaced = N.c_int(0)
+    N.call(
+        "dm_size_from_velocity", D.ptr(vpd), vpd.numel(), shape[1] * (shape[2] if dim == 3 else 1),
+        D.ptr(gterm), scale, float(sz_opts["vp_water"] or 0.0), float(sz_opts["wl"]),
+        float(sz_opts["freq"]), float(sz_opts["grad"]), float(sz_opts["hmin"]),
+        float(sz_opts["hmax"]), float(sz_opts["dt"]), float(sz_opts["cr_max"]),
+        float(sz_opts["space_order"]), dim, D.ptr(cell), replaced, D.ptr(ws), ws.numel(),
+        D.stream_ptr(),
+    )
+    grade = sz_opts["grade"]
+    if grade == 0.0:
+        warnings.warn("Mesh size gradient is deactiavted. This may compromise mesh quality")
+    else:
+        if grade < 0:
+            raise ValueError("Parameter `grade` must be > 0.0")
+        if grade > 1.0:
+            warnings.warn("Parameter `grade` is set pretty high (> 1.0)!")
+        print(f"Enforcing mesh size gradation of {grade} decimal percent...")
+        elen = (bbox[1] - bbox[0]) / nz
+        # a C-order (n0, n1[, n2]) array is the column-major array with the
+        # axes reversed; the limiter is symmetric in the axes
+        dims = (N.c_int * 3)(*(list(shape[::-1]) + [1] * (3 - dim)))
+        N.call("dm_limgrad", dims, float(elen), float(grade), 10000, D.ptr(cell), D.stream_ptr())
+
+    cell, vpd, bbox = _build_domain_pad(cell, vpd, bbox, sz_opts)
+    fh = GridSizing.from_device(cell, bbox)
+    return SizeFunction(bbox, fh, sz_opts["hmin"])
+
+
+def _get_dimensions(shape, bbox):
+    dim = len(shape)
+    return [(bbox[2 * k + 1] - bbox[2 * k]) / shape[k] for k in range(dim)]
+
+
+def _build_domain_pad(cell, vp, bbox, opts):
+    """domain extension (sizing/mesh_size_function.py:526-572) on the GPU"""
+    dim = cell.dim()
+    domain_pad = opts["domain_pad"]
+    pad_style = opts["pad_style"]
+    if domain_pad < 0:
+        raise ValueError("Domain extension must be >= 0")
+    if domain_pad <= 0:
+        return cell, vp, bbox
+    print(f"Including a {domain_pad} meter domain extension...")
+    d = _get_dimensions(tuple(cell.shape), bbox)
+    nn = [int(domain_pad / dk) for dk in d]
+    if dim == 2:
+        bbox = (bbox[0] - domain_pad, bbox[1], bbox[2] - domain_pad, bbox[3] + domain_pad)
+        pre, post = [nn[0], nn[1]], [0, nn[1]]
+    else:
+        bbox = (
+            bbox[0] - domain_pad, bbox[1], bbox[2] - domain_pad, bbox[3] + domain_pad,
+            bbox[4] - domain_pad, bbox[5] + domain_pad,
+        )
+        pre, post = [nn[0], nn[1], nn[2]], [0, nn[1], nn[2]]
+    print(f"Using the pad_style: {pad_style}")
+    modes = {"edge": 0, "constant": 1, "linear_ramp": 2}
+    if pad_style not in modes:
+        raise ValueError(
+            "pad style currently not supported. Try `linear_ramp`, `edge`, or `constant`"
+        )
+
+    def pad(a):
+        cval = float(a.max().item())
+        out_shape = [a.shape[k] + pre[k] + post[k] for k in range(dim)]
+        out = D.empty(out_shape, torch.float64)
+        n = (N.c_int * 3)(*list(a.shape))
+        pr = (N.c_int * 3)(*pre)
+        po = (N.c_int * 3)(*post)
+        N.call("dm_pad_grid", D.ptr(a), n, pr, po, dim, modes[pad_style], cval, D.ptr(out), D.stream_ptr())
+        return out
+
+    return pad(cell), pad(vp), bbox
+
+
+def read_velocity_model(
+    filename, nz=None, nx=None, ny=None, byte_order=None, axes_order=None,
+    axes_order_sort=None, dtype=None,
+):
+    """Read a velocity model (sizing/mesh_size_function.py:590-606)."""
+    if filename.endswith(".segy"):
+        return _read_segy(filename)
+    return _read_bin(filename, nz, nx, ny, byte_order, axes_order, axes_order_sort, dtype)
+
+
+def _read_bin(filename, nz, nx, ny, byte_order, axes_order, axes_order_sort, dtype):
+    """Binary model with endianness, axis order and F/C order
+    (sizing/mesh_size_function.py:609-630)."""
+    if (nz is None) or (nx is None) or (ny is None):
+        raise ValueError(
+            "Please specify the number of grid points in each dimension (e.g., `nz`, `nx`, `ny`)..."
+        )
+    axes = [nz, nx, ny]
+    ix = np.argsort(axes_order)
+    axes = [axes[o] for o in ix]
+    print(f"Reading binary file: {filename}")
+    if byte_order == "big":
+        vp = np.fromfile(filename, dtype=np.dtype(dtype).newbyteorder(">"))
+    elif byte_order == "little":
+        vp = np.fromfile(filename, dtype=np.dtype(dtype).newbyteorder("<"))
+    else:
+        raise ValueError("Please specify byte_order as either: little or big.")
+    vp = vp.reshape(*axes, order=axes_order_sort)
+    vp = np.flipud(vp.transpose((*axes_order,)))
+    return vp, nz, nx, ny
+
+
+def _ibm_to_ieee(words):
+    """IBM System/360 single precision (SEG-Y format code 1) to float64:
+    sign bit, 7-bit base-16 exponent biased by 64, 24-bit fraction."""
+    w = words.astype(np.uint32)
+    sign = np.where(w >> 31, -1.0, 1.0)
+    expo = ((w >> 24) & 0x7F).astype(np.int64) - 64
+    frac = (w & 0x00FFFFFF).astype(np.float64) / float(1 << 24)
+    return sign * frac * np.power(16.0, expo)
+
+
+def _read_segy(filename):
+    """SEG-Y reader (sizing/mesh_size_function.py:633-646) without segyio:
+    3200-byte text header, 400-byte binary header (samples per trace at
+    bytes 3221-3222, format code at 3225-3226), then traces of a 240-byte
+    header plus samples.  Format codes 1 (IBM float) and 5 (IEEE float)."""
+    raw = np.fromfile(filename, dtype=np.uint8)
+    ns = int.from_bytes(raw[3220:3222].tobytes(), "big")
+    fmt = int.from_bytes(raw[3224:3226].tobytes(), "big")
+    if fmt not in (1, 5):
+        raise NotImplementedError(f"SEG-Y sample format {fmt} is not supported")
+    body = raw[3600:]
+    tr_bytes = 240 + 4 * ns
+    nx = len(body) // tr_bytes
+    traces = body[: nx * tr_bytes].reshape(nx, tr_bytes)[:, 240:]
+    words = traces.copy().view(">u4").reshape(nx, ns)
+    if fmt == 1:
+        vals = _ibm_to_ieee(words)
+    else:
+        vals = words.view(">f4").astype(np.float64)
+    vp = np.ascontiguousarray(vals.T)
+    if np.amin(vp) < 1000.0:
+        warnings.warn("Velocity appear to be in km/s. Maybe pass `units` km-s key pair?")
+    return np.flipud(vp), ns, nx, 0
+
+
+def write_velocity_model(*args, **kwargs):
+    """HDF5 writer of the reference (242-335); needs h5py, absent here."""
+    try:
+        import h5py  # noqa: F401
+    except ImportError as e:
+        raise ImportError("write_velocity_model needs h5py") from e
+    raise NotImplementedError("write_velocity_model is outside the GPU engine")
+
+
+def plot_sizing_function(*args, **kwargs):
+    raise NotImplementedError("plotting is not part of the GPU engine")
