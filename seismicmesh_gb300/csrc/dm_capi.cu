@@ -89,20 +89,24 @@ const char *dm_last_error(void) { return dm::last_error(); }
 int dm_abi_count(void) { return 37; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
-  return dmp::orient2(a, b, c);
+  dmp::ExactScratch W;
+  return dmp::orient2(a, b, c, &W);
 }
 int dm_orient3(const float *a, const float *b, const float *c, const float *d) {
-  return dmp::orient3(a, b, c, d);
+  dmp::ExactScratch W;
+  return dmp::orient3(a, b, c, d, &W);
 }
 int dm_incircle_sos(const float *a, const float *b, const float *c,
                     const float *d) {
   int ovf = 0;
-  return dmp::incirc2_sos(a, b, c, d, &ovf);
+  dmp::ExactScratch W;
+  return dmp::incirc2_sos(a, b, c, d, &ovf, &W);
 }
 int dm_insphere_sos(const float *a, const float *b, const float *c,
                     const float *d, const float *e) {
   int ovf = 0;
-  return dmp::insph3_sos(a, b, c, d, e, &ovf);
+  dmp::ExactScratch W;
+  return dmp::insph3_sos(a, b, c, d, e, &ovf, &W);
 }
 
 int dm_delaunay_workspace_size(int32_t dim, int64_t n, size_t *bytes) {
@@ -320,3 +324,21 @@ int dm_pad_grid(const double *src, const int32_t *n_host,
 }
 
 }  // extern "C"
+
+// Debug aid (not part of the public ABI): host evaluation of the individual
+// predicate stages (0 orient3_exact, 1 orient3_slow, 2 insph3_exact,
+// 3 insph3_slow, 4 orient2_exact, 5 incirc2_exact).
+extern "C" int dmdbg_host_pred(int kind, const float *a, const float *b,
+                               const float *c, const float *d, const float *e) {
+  int ovf = 0;
+  dmp::ExactScratch W;
+  switch (kind) {
+    case 0: return dmp::orient3_exact(a, b, c, d, &W);
+    case 1: return dmp::orient3_slow(a, b, c, d, &W);
+    case 2: return dmp::insph3_exact(a, b, c, d, e, &ovf, &W);
+    case 3: return dmp::insph3_slow(a, b, c, d, e, &ovf, &W);
+    case 4: return dmp::orient2_exact(a, b, c, &W);
+    case 5: return dmp::incirc2_exact(a, b, c, d, &ovf, &W);
+  }
+  return -99;
+}

@@ -354,7 +354,7 @@ __device__ __forceinline__ void warp_argmin(float &key, int &j, int &gid) {
 
 // ---- 3D level-1 predicates on shared candidates (p is the origin)
 __device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
-                                   int a, int b, int c) {
+                                   int a, int b, int c, dmp::ExactScratch *W) {
   float4 A = S.c[a], B = S.c[b], C = S.c[c];
   int s = dmp::orient3_rel_filter<float>(A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
                                          C.z, 16.0f * DMP_U32);
@@ -364,15 +364,16 @@ __device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
   load_pt<3>(P, S.id[a], ar);
   load_pt<3>(P, S.id[b], br);
   load_pt<3>(P, S.id[c], cr);
-  return dmp::orient3_slow(pr, ar, br, cr);
+  return dmp::orient3_slow(pr, ar, br, cr, W);
 }
 
 __device__ __forceinline__ int is3L(const WarpL1<3> &S, const float *P, int ip,
-                                    int a, int b, int c, int d, int &ovf) {
+                                    int a, int b, int c, int d, int &ovf,
+                                    dmp::ExactScratch *W) {
   float4 A = S.c[a], B = S.c[b], C = S.c[c], D = S.c[d];
   float X[3] = {A.x, A.y, A.z}, Y[3] = {B.x, B.y, B.z}, Z[3] = {C.x, C.y, C.z},
-        W[3] = {D.x, D.y, D.z};
-  int s = dmp::insph3_rel_filter<float>(X, Y, Z, W, A.w, B.w, C.w, D.w,
+        Q[3] = {D.x, D.y, D.z};
+  int s = dmp::insph3_rel_filter<float>(X, Y, Z, Q, A.w, B.w, C.w, D.w,
                                         48.0f * DMP_U32);
   if (s) return s;
   float pr[3], ar[3], br[3], cr[3], dr[3];
@@ -381,13 +382,14 @@ __device__ __forceinline__ int is3L(const WarpL1<3> &S, const float *P, int ip,
   load_pt<3>(P, S.id[b], br);
   load_pt<3>(P, S.id[c], cr);
   load_pt<3>(P, S.id[d], dr);
-  return insph3_sos(pr, ar, br, cr, dr, &ovf);
+  return insph3_sos(pr, ar, br, cr, dr, &ovf, W);
 }
 
 // gift-wrap query on face (p, a, b): winner among candidates y with
 // orient3(p,a,b,y) > 0 whose sphere through the face is smallest; -1 if none.
-__device__ int gw3L(const WarpL1<3> &S, const float *P, int ip, int a, int b,
-                    int lane, int &ovf) {
+__device__ __forceinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
+                                    int a, int b, int lane, int &ovf,
+                                    dmp::ExactScratch *W) {
   const int nc = S.nc;
   float4 A = S.c[a], B = S.c[b];
   float nx = A.y * B.z - A.z * B.y, ny = A.z * B.x - A.x * B.z,
@@ -405,7 +407,7 @@ __device__ int gw3L(const WarpL1<3> &S, const float *P, int ip, int a, int b,
   for (int s = 0; s < L1<3>::PER; ++s) {
     int j = lane + 32 * s;
     if (j < nc && j != a && j != b) {
-      if (o3L(S, P, ip, a, b, j) > 0) {
+      if (o3L(S, P, ip, a, b, j, W) > 0) {
         pos |= 1u << s;
         float4 Y = S.c[j];
         float den = Y.x * nx + Y.y * ny + Y.z * nz;
@@ -428,7 +430,7 @@ __device__ int gw3L(const WarpL1<3> &S, const float *P, int ip, int a, int b,
     for (int s = 0; s < L1<3>::PER; ++s) {
       int j = lane + 32 * s;
       if (found < 0 && (pos >> s & 1u) && j != bj) {
-        if (is3L(S, P, ip, a, b, bj, j, ovf) < 0) found = j;
+        if (is3L(S, P, ip, a, b, bj, j, ovf, W) < 0) found = j;
       }
     }
     unsigned m = __ballot_sync(0xffffffffu, found >= 0);
@@ -476,7 +478,7 @@ __device__ __forceinline__ bool certified3(float4 A, float4 B, float4 C,
 }
 
 template <int DIM>
-__device__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const GridParams &g,
+__device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const GridParams &g,
                           int ip, const float *px, int lane) {
   constexpr int K = L1<DIM>::K, W = 2 * K + 1;
   constexpr int NCELL = DIM == 3 ? W * W * W : W * W;
@@ -577,8 +579,9 @@ __device__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const GridParams &g,
 }
 
 // seed search (3D): returns packed link triangle or 0xffffffff
-__device__ uint32_t seed3L(const WarpL1<3> &S, const float *P, int ip, int lane,
-                           int &ovf) {
+__device__ __forceinline__ uint32_t seed3L(const WarpL1<3> &S, const float *P,
+                                           int ip, int lane, int &ovf,
+                                           dmp::ExactScratch *W) {
   const int nc = S.nc;
   float pk1 = -1.f;
   int pg1 = -1;
@@ -632,11 +635,11 @@ __device__ uint32_t seed3L(const WarpL1<3> &S, const float *P, int ip, int lane,
       pk2 = ck;
       pg2 = cg;
       int q2 = cj;
-      int xp = gw3L(S, P, ip, q1, q2, lane, ovf);
-      int xm = gw3L(S, P, ip, q2, q1, lane, ovf);
+      int xp = gw3L(S, P, ip, q1, q2, lane, ovf, W);
+      int xm = gw3L(S, P, ip, q2, q1, lane, ovf, W);
       if (xp < 0 && xm < 0) continue;
       bool ok = true;
-      if (xp >= 0 && xm >= 0) ok = is3L(S, P, ip, q1, q2, xp, xm, ovf) > 0;
+      if (xp >= 0 && xm >= 0) ok = is3L(S, P, ip, q1, q2, xp, xm, ovf, W) > 0;
       if (ok) return xp >= 0 ? pack3(q1, q2, xp) : pack3(q2, q1, xm);
     }
   }
@@ -644,11 +647,9 @@ __device__ uint32_t seed3L(const WarpL1<3> &S, const float *P, int ip, int lane,
 }
 
 // seed search (2D): link edge (a, b) of a positive triangle (p, a, b)
-__device__ int gw2L(const WarpL1<2> &S, const float *P, int ip, int x, int sgn,
-                    int lane, int &ovf);
 
 __device__ __forceinline__ int o2L(const WarpL1<2> &S, const float *P, int ip,
-                                   int a, int b) {
+                                   int a, int b, dmp::ExactScratch *W) {
   float4 A = S.c[a], B = S.c[b];
   int s = dmp::orient2_rel_filter<float>(A.x, A.y, B.x, B.y, 8.0f * DMP_U32);
   if (s) return s;
@@ -656,12 +657,13 @@ __device__ __forceinline__ int o2L(const WarpL1<2> &S, const float *P, int ip,
   load_pt<2>(P, ip, pr);
   load_pt<2>(P, S.id[a], ar);
   load_pt<2>(P, S.id[b], br);
-  return dmp::orient2_slow(pr, ar, br);
+  return dmp::orient2_slow(pr, ar, br, W);
 }
 
 // incirc2(p, a, b, d)
 __device__ __forceinline__ int ic2L(const WarpL1<2> &S, const float *P, int ip,
-                                    int a, int b, int d, int &ovf) {
+                                    int a, int b, int d, int &ovf,
+                                    dmp::ExactScratch *W) {
   float4 A = S.c[a], B = S.c[b], D = S.c[d];
   float X[2] = {A.x, A.y}, Y[2] = {B.x, B.y}, Z[2] = {D.x, D.y};
   int s = dmp::incirc2_rel_filter<float>(X, Y, Z, A.w, B.w, D.w, 16.0f * DMP_U32);
@@ -671,14 +673,15 @@ __device__ __forceinline__ int ic2L(const WarpL1<2> &S, const float *P, int ip,
   load_pt<2>(P, S.id[a], ar);
   load_pt<2>(P, S.id[b], br);
   load_pt<2>(P, S.id[d], dr);
-  return incirc2_sos(pr, ar, br, dr, &ovf);
+  return incirc2_sos(pr, ar, br, dr, &ovf, W);
 }
 
 // 2D gift-wrap across edge (p, x): sgn=+1 candidates with orient2(p,x,y)>0
 // (triangle (p,x,y)); sgn=-1 candidates with orient2(p,y,x)>0 (triangle
 // (p,y,x)).  Winner has the smallest circle through p and x on that side.
-__device__ int gw2L(const WarpL1<2> &S, const float *P, int ip, int x, int sgn,
-                    int lane, int &ovf) {
+__device__ __forceinline__ int gw2L(const WarpL1<2> &S, const float *P, int ip,
+                                    int x, int sgn, int lane, int &ovf,
+                                    dmp::ExactScratch *W) {
   const int nc = S.nc;
   float4 X = S.c[x];
   float nx = -X.y * sgn, ny = X.x * sgn;
@@ -689,7 +692,7 @@ __device__ int gw2L(const WarpL1<2> &S, const float *P, int ip, int x, int sgn,
   for (int s = 0; s < L1<2>::PER; ++s) {
     int j = lane + 32 * s;
     if (j < nc && j != x) {
-      int o = sgn > 0 ? o2L(S, P, ip, x, j) : o2L(S, P, ip, j, x);
+      int o = sgn > 0 ? o2L(S, P, ip, x, j, W) : o2L(S, P, ip, j, x, W);
       if (o > 0) {
         pos |= 1u << s;
         float4 Y = S.c[j];
@@ -713,7 +716,7 @@ __device__ int gw2L(const WarpL1<2> &S, const float *P, int ip, int x, int sgn,
     for (int s = 0; s < L1<2>::PER; ++s) {
       int j = lane + 32 * s;
       if (found < 0 && (pos >> s & 1u) && j != bj) {
-        int r = sgn > 0 ? ic2L(S, P, ip, x, bj, j, ovf) : ic2L(S, P, ip, bj, x, j, ovf);
+        int r = sgn > 0 ? ic2L(S, P, ip, x, bj, j, ovf, W) : ic2L(S, P, ip, bj, x, j, ovf, W);
         if (r < 0) found = j;
       }
     }
@@ -734,8 +737,9 @@ __device__ __forceinline__ bool certified2(float4 A, float4 B, float reff) {
 }
 
 // 2D seed: returns packed (q1, x) with triangle (p, q1, x) positive, or ~0
-__device__ uint32_t seed2L(const WarpL1<2> &S, const float *P, int ip, int lane,
-                           int &ovf) {
+__device__ __forceinline__ uint32_t seed2L(const WarpL1<2> &S, const float *P,
+                                           int ip, int lane, int &ovf,
+                                           dmp::ExactScratch *W) {
   const int nc = S.nc;
   float pk = -1.f;
   int pg = -1;
@@ -759,11 +763,11 @@ __device__ uint32_t seed2L(const WarpL1<2> &S, const float *P, int ip, int lane,
     pk = bk;
     pg = bg;
     int q1 = bj;
-    int xp = gw2L(S, P, ip, q1, +1, lane, ovf);
-    int xm = gw2L(S, P, ip, q1, -1, lane, ovf);
+    int xp = gw2L(S, P, ip, q1, +1, lane, ovf, W);
+    int xm = gw2L(S, P, ip, q1, -1, lane, ovf, W);
     if (xp < 0 && xm < 0) continue;
     bool ok = true;
-    if (xp >= 0 && xm >= 0) ok = ic2L(S, P, ip, q1, xp, xm, ovf) > 0;
+    if (xp >= 0 && xm >= 0) ok = ic2L(S, P, ip, q1, xp, xm, ovf, W) > 0;
     if (ok) return xp >= 0 ? pack3(q1, xp, 0) : pack3(xm, q1, 0);
   }
   return 0xffffffffu;
@@ -782,6 +786,8 @@ __device__ __forceinline__ void escalate(const DTArgs &A, int p, int4 seed,
 
 __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
   __shared__ WarpL1<3> sm[L1_WARPS];
+  dmp::ExactScratch WS;
+  dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpL1<3> &S = sm[w];
   const GridParams g = *A.gp;
@@ -793,7 +799,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
     load_pt<3>(A.P, ip, px);
     gather_l1<3>(S, A, g, ip, px, lane);
     int ovf = 0;
-    uint32_t seed = S.nc >= 3 ? seed3L(S, A.P, ip, lane, ovf) : 0xffffffffu;
+    uint32_t seed = S.nc >= 3 ? seed3L(S, A.P, ip, lane, ovf, W) : 0xffffffffu;
     if (seed == 0xffffffffu) {
       escalate(A, ip, make_int4(ip, -1, -1, -1), lane);
       continue;
@@ -816,7 +822,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
       if (lane == 0) S.nopen--;
       __syncwarp();
       int u = un0(e), v = un1(e);
-      int y = gw3L(S, A.P, ip, v, u, lane, ovf);
+      int y = gw3L(S, A.P, ip, v, u, lane, ovf, W);
       if (y < 0) {
         hull = 1;
         continue;
@@ -898,6 +904,8 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
 
 __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
   __shared__ WarpL1<2> sm[L1_WARPS];
+  dmp::ExactScratch WS;
+  dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpL1<2> &S = sm[w];
   const GridParams g = *A.gp;
@@ -909,7 +917,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
     load_pt<2>(A.P, ip, px);
     gather_l1<2>(S, A, g, ip, px, lane);
     int ovf = 0;
-    uint32_t seed = S.nc >= 2 ? seed2L(S, A.P, ip, lane, ovf) : 0xffffffffu;
+    uint32_t seed = S.nc >= 2 ? seed2L(S, A.P, ip, lane, ovf, W) : 0xffffffffu;
     if (seed == 0xffffffffu) {
       escalate(A, ip, make_int4(ip, -1, -1, -1), lane);
       continue;
@@ -922,16 +930,23 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
       S.flags = 0;
     }
     __syncwarp();
-    bool closed = false, hull = false;
+    bool hull = false;
     int cur = b;
     while (true) {
-      int nx = gw2L(S, A.P, ip, cur, +1, lane, ovf);
+      int nx = gw2L(S, A.P, ip, cur, +1, lane, ovf, W);
       if (nx < 0) {
         hull = true;
         break;
       }
+      if (S.ntri >= L1<2>::MAXTRI) {
+        if (lane == 0) S.flags |= 1;
+        __syncwarp();
+        break;
+      }
       if (nx == a) {
-        closed = true;
+        // closing triangle (p, cur, a)
+        if (lane == 0) S.tri[S.ntri++] = pack3(cur, nx, 0);
+        __syncwarp();
         break;
       }
       if (S.ntri >= L1<2>::MAXTRI) {
@@ -946,7 +961,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
     if (hull && !S.flags) {
       cur = a;
       while (true) {
-        int pv2 = gw2L(S, A.P, ip, cur, -1, lane, ovf);
+        int pv2 = gw2L(S, A.P, ip, cur, -1, lane, ovf, W);
         if (pv2 < 0) break;
         if (S.ntri >= L1<2>::MAXTRI) {
           if (lane == 0) S.flags |= 1;
@@ -958,7 +973,6 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
         cur = pv2;
       }
     }
-    (void)closed;
     bool allok = !hull && !S.flags;
     int cert_any = -1;
     for (int t = lane; t < S.ntri; t += 32) {
@@ -1030,21 +1044,23 @@ struct Face3 {
   float V[3], U[3], n[3];
 };
 
-__device__ __forceinline__ int side3(const Face3 &F, const float *y) {
+__device__ __forceinline__ int side3(const Face3 &F, const float *y,
+                                     dmp::ExactScratch *W) {
   float Y[3] = {y[0] - F.p[0], y[1] - F.p[1], y[2] - F.p[2]};
   int s = dmp::orient3_rel_filter<float>(F.V[0], F.V[1], F.V[2], F.U[0], F.U[1],
                                          F.U[2], Y[0], Y[1], Y[2], 16.0f * DMP_U32);
   if (s) return s;
-  return dmp::orient3_slow(F.p, F.a, F.b, y);
+  return dmp::orient3_slow(F.p, F.a, F.b, y, W);
 }
 
 __device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j,
-                                          int &best, float *bx, int &ovf) {
+                                          int &best, float *bx, int &ovf,
+                                          dmp::ExactScratch *W) {
   if (j == F.ip || j == F.ia || j == F.ib || A.dup[j]) return;
   float y[3];
   load_pt<3>(A.P, j, y);
-  if (side3(F, y) <= 0) return;
-  if (best < 0 || insph3_sos(F.p, F.a, F.b, bx, y, &ovf) < 0) {
+  if (side3(F, y, W) <= 0) return;
+  if (best < 0 || insph3_sos(F.p, F.a, F.b, bx, y, &ovf, W) < 0) {
     best = j;
     bx[0] = y[0];
     bx[1] = y[1];
@@ -1053,7 +1069,8 @@ __device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j
 }
 
 __device__ __forceinline__ int tourney3(const DTArgs &A, const Face3 &F,
-                                        int best, int &ovf) {
+                                        int best, int &ovf,
+                                        dmp::ExactScratch *W) {
   for (int o = 16; o; o >>= 1) {
     int other = __shfl_xor_sync(0xffffffffu, best, o);
     if (other >= 0 && other != best) {
@@ -1063,7 +1080,7 @@ __device__ __forceinline__ int tourney3(const DTArgs &A, const Face3 &F,
         float bx[3], ox[3];
         load_pt<3>(A.P, best, bx);
         load_pt<3>(A.P, other, ox);
-        if (insph3_sos(F.p, F.a, F.b, bx, ox, &ovf) < 0) best = other;
+        if (insph3_sos(F.p, F.a, F.b, bx, ox, &ovf, W) < 0) best = other;
       }
     }
   }
@@ -1082,8 +1099,9 @@ __device__ __forceinline__ void for_cell(const DTArgs &A, int c, F f) {
 }
 
 // exhaustive gift-wrap query on face (p, a, b), 3D
-__device__ int gq3(const DTArgs &A, const GridParams &g, int ip, int ia, int ib,
-                   int lane, int &ovf) {
+__device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
+                                   int ia, int ib, int lane, int &ovf,
+                                   dmp::ExactScratch *W) {
   Face3 F;
   F.ip = ip;
   F.ia = ia;
@@ -1108,9 +1126,9 @@ __device__ int gq3(const DTArgs &A, const GridParams &g, int ip, int ia, int ib,
         z = cc[2] + lane / 9 - 1;
     if (x >= 0 && y >= 0 && z >= 0 && x < g.dims[0] && y < g.dims[1] && z < g.dims[2])
       for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-               [&](int j) { consider3(A, F, j, best, bx, ovf); });
+               [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
   }
-  best = tourney3(A, F, best, ovf);
+  best = tourney3(A, F, best, ovf, W);
   // search region
   bool full = true;
   double cen[3] = {0, 0, 0}, rad = 0;
@@ -1168,7 +1186,7 @@ __device__ int gq3(const DTArgs &A, const GridParams &g, int ip, int ia, int ib,
         }
         if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
         for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                 [&](int j) { consider3(A, F, j, best, bx, ovf); });
+                 [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
       }
     } else {
       int blo[3], bhi[3];
@@ -1197,7 +1215,7 @@ __device__ int gq3(const DTArgs &A, const GridParams &g, int ip, int ia, int ib,
             for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
               if (in_local(cc, x, y, z, 3)) continue;
               for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                       [&](int j) { consider3(A, F, j, best, bx, ovf); });
+                       [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
             }
       }
     }
@@ -1224,11 +1242,11 @@ __device__ int gq3(const DTArgs &A, const GridParams &g, int ip, int ia, int ib,
           for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
             if (in_local(cc, x, y, z, 3)) continue;
             for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                     [&](int j) { consider3(A, F, j, best, bx, ovf); });
+                     [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
           }
     }
   }
-  return tourney3(A, F, best, ovf);
+  return tourney3(A, F, best, ovf, W);
 }
 
 // ---- 2D exhaustive query across edge (p, x): sgn=+1 triangles (p,x,y),
@@ -1239,27 +1257,30 @@ struct Edge2 {
   float X[2];
 };
 
-__device__ __forceinline__ int side2(const Edge2 &E, const float *y) {
+__device__ __forceinline__ int side2(const Edge2 &E, const float *y,
+                                     dmp::ExactScratch *W) {
   float Y[2] = {y[0] - E.p[0], y[1] - E.p[1]};
   int s = dmp::orient2_rel_filter<float>(E.X[0], E.X[1], Y[0], Y[1], 8.0f * DMP_U32);
-  if (!s) s = dmp::orient2_slow(E.p, E.x, y);
+  if (!s) s = dmp::orient2_slow(E.p, E.x, y, W);
   return s * E.sgn;
 }
 
 __device__ __forceinline__ int cmp2(const Edge2 &E, const float *bx,
-                                    const float *y, int &ovf) {
+                                    const float *y, int &ovf,
+                                    dmp::ExactScratch *W) {
   // <0 when y lies inside the circle of the current triangle
-  return E.sgn > 0 ? incirc2_sos(E.p, E.x, bx, y, &ovf)
-                   : incirc2_sos(E.p, bx, E.x, y, &ovf);
+  return E.sgn > 0 ? incirc2_sos(E.p, E.x, bx, y, &ovf, W)
+                   : incirc2_sos(E.p, bx, E.x, y, &ovf, W);
 }
 
 __device__ __forceinline__ void consider2(const DTArgs &A, const Edge2 &E, int j,
-                                          int &best, float *bx, int &ovf) {
+                                          int &best, float *bx, int &ovf,
+                                          dmp::ExactScratch *W) {
   if (j == E.ip || j == E.ix || A.dup[j]) return;
   float y[2];
   load_pt<2>(A.P, j, y);
-  if (side2(E, y) <= 0) return;
-  if (best < 0 || cmp2(E, bx, y, ovf) < 0) {
+  if (side2(E, y, W) <= 0) return;
+  if (best < 0 || cmp2(E, bx, y, ovf, W) < 0) {
     best = j;
     bx[0] = y[0];
     bx[1] = y[1];
@@ -1267,7 +1288,8 @@ __device__ __forceinline__ void consider2(const DTArgs &A, const Edge2 &E, int j
 }
 
 __device__ __forceinline__ int tourney2(const DTArgs &A, const Edge2 &E,
-                                        int best, int &ovf) {
+                                        int best, int &ovf,
+                                        dmp::ExactScratch *W) {
   for (int o = 16; o; o >>= 1) {
     int other = __shfl_xor_sync(0xffffffffu, best, o);
     if (other >= 0 && other != best) {
@@ -1277,15 +1299,16 @@ __device__ __forceinline__ int tourney2(const DTArgs &A, const Edge2 &E,
         float bx[2], ox[2];
         load_pt<2>(A.P, best, bx);
         load_pt<2>(A.P, other, ox);
-        if (cmp2(E, bx, ox, ovf) < 0) best = other;
+        if (cmp2(E, bx, ox, ovf, W) < 0) best = other;
       }
     }
   }
   return best;
 }
 
-__device__ int gq2(const DTArgs &A, const GridParams &g, int ip, int ix, int sgn,
-                   int lane, int &ovf) {
+__device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
+                                   int ix, int sgn, int lane, int &ovf,
+                                   dmp::ExactScratch *W) {
   Edge2 E;
   E.ip = ip;
   E.ix = ix;
@@ -1301,9 +1324,9 @@ __device__ int gq2(const DTArgs &A, const GridParams &g, int ip, int ix, int sgn
   if (lane < 9) {
     int x = cc[0] + lane % 3 - 1, y = cc[1] + lane / 3 - 1;
     if (x >= 0 && y >= 0 && x < g.dims[0] && y < g.dims[1])
-      for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+      for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
   }
-  best = tourney2(A, E, best, ovf);
+  best = tourney2(A, E, best, ovf, W);
   bool full = true;
   double cen[2] = {0, 0}, rad = 0;
   if (best >= 0) {
@@ -1346,7 +1369,7 @@ __device__ int gq2(const DTArgs &A, const GridParams &g, int ip, int ix, int sgn
           dd += e * e;
         }
         if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
-        for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+        for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
       }
     } else {
       int blo[2] = {lo[0] / g.bs, lo[1] / g.bs}, bhi[2] = {hi[0] / g.bs, hi[1] / g.bs};
@@ -1367,7 +1390,7 @@ __device__ int gq2(const DTArgs &A, const GridParams &g, int ip, int ix, int sgn
         for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
           for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
             if (in_local(cc, x, y, 0, 2)) continue;
-            for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+            for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
           }
       }
     }
@@ -1388,11 +1411,11 @@ __device__ int gq2(const DTArgs &A, const GridParams &g, int ip, int ix, int sgn
       for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
         for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
           if (in_local(cc, x, y, 0, 2)) continue;
-          for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf); });
+          for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
         }
     }
   }
-  return tourney2(A, E, best, ovf);
+  return tourney2(A, E, best, ovf, W);
 }
 
 __device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane) {
@@ -1408,6 +1431,8 @@ __device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane
 
 __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
+  dmp::ExactScratch WS;
+  dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpL2 &S = sm[w];
   const GridParams g = *A.gp;
@@ -1425,8 +1450,8 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
       int f[3][2] = {{sd.y, sd.z}, {sd.z, sd.w}, {sd.w, sd.y}};
       for (int t = 0; t < 3 && seed.x < 0; ++t) {
         int a = f[t][0], b = f[t][1];
-        int xp = gq3(A, g, ip, a, b, lane, ovf);
-        int xm = gq3(A, g, ip, b, a, lane, ovf);
+        int xp = gq3(A, g, ip, a, b, lane, ovf, W);
+        int xm = gq3(A, g, ip, b, a, lane, ovf, W);
         if (xp < 0 && xm < 0) continue;
         bool ok = true;
         if (xp >= 0 && xm >= 0) {
@@ -1436,7 +1461,7 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
           load_pt<3>(A.P, b, br);
           load_pt<3>(A.P, xp, xr);
           load_pt<3>(A.P, xm, mr);
-          ok = insph3_sos(pr, ar, br, xr, mr, &ovf) > 0;
+          ok = insph3_sos(pr, ar, br, xr, mr, &ovf, W) > 0;
         }
         if (ok) seed = xp >= 0 ? make_int3(a, b, xp) : make_int3(b, a, xm);
       }
@@ -1461,7 +1486,7 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
       if (lane == 0) S.nopen--;
       __syncwarp();
       int u = e.x, v = e.y;
-      int y = gq3(A, g, ip, v, u, lane, ovf);
+      int y = gq3(A, g, ip, v, u, lane, ovf, W);
       if (y < 0) continue;  // convex-hull face
       if (S.ntri >= L2_MAXTRI) {
         if (lane == 0) S.flags |= 1;
@@ -1487,7 +1512,12 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
       }
       if (S.flags) break;
     }
-    if (S.flags && lane == 0) flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+    if (S.flags && lane == 0) {
+      flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+      A.counters[8] = ip;
+      A.counters[9] = S.ntri;
+      A.counters[10] = S.nopen;
+    }
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
     for (int t0 = 0; t0 < S.ntri; t0 += 32) {
       int t = t0 + lane;
@@ -1512,6 +1542,8 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
 
 __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
+  dmp::ExactScratch WS;
+  dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpL2 &S = sm[w];
   const GridParams g = *A.gp;
@@ -1532,8 +1564,8 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
       for (int t = 0; t < 2 && a < 0; ++t) {
         int q1 = cand[t];
         if (q1 < 0) continue;
-        int xp = gq2(A, g, ip, q1, +1, lane, ovf);
-        int xm = gq2(A, g, ip, q1, -1, lane, ovf);
+        int xp = gq2(A, g, ip, q1, +1, lane, ovf, W);
+        int xm = gq2(A, g, ip, q1, -1, lane, ovf, W);
         if (xp < 0 && xm < 0) continue;
         bool ok = true;
         if (xp >= 0 && xm >= 0) {
@@ -1542,7 +1574,7 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
           load_pt<2>(A.P, q1, qr);
           load_pt<2>(A.P, xp, xr);
           load_pt<2>(A.P, xm, mr);
-          ok = incirc2_sos(pr, qr, xr, mr, &ovf) > 0;
+          ok = incirc2_sos(pr, qr, xr, mr, &ovf, W) > 0;
         }
         if (ok) {
           if (xp >= 0) {
@@ -1568,12 +1600,21 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
     bool hull = false;
     int cur = b;
     while (true) {
-      int nx = gq2(A, g, ip, cur, +1, lane, ovf);
+      int nx = gq2(A, g, ip, cur, +1, lane, ovf, W);
       if (nx < 0) {
         hull = true;
         break;
       }
-      if (nx == a) break;
+      if (S.ntri >= L2_MAXTRI) {
+        if (lane == 0) S.flags |= 1;
+        __syncwarp();
+        break;
+      }
+      if (nx == a) {
+        if (lane == 0) S.tri[S.ntri++] = make_int3(cur, nx, 0);
+        __syncwarp();
+        break;
+      }
       if (S.ntri >= L2_MAXTRI) {
         if (lane == 0) S.flags |= 1;
         __syncwarp();
@@ -1586,7 +1627,7 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
     if (hull && !S.flags) {
       cur = a;
       while (true) {
-        int pv = gq2(A, g, ip, cur, -1, lane, ovf);
+        int pv = gq2(A, g, ip, cur, -1, lane, ovf, W);
         if (pv < 0) break;
         if (S.ntri >= L2_MAXTRI) {
           if (lane == 0) S.flags |= 1;
@@ -1598,7 +1639,12 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
         cur = pv;
       }
     }
-    if (S.flags && lane == 0) flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+    if (S.flags && lane == 0) {
+      flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+      A.counters[8] = ip;
+      A.counters[9] = S.ntri;
+      A.counters[10] = S.nopen;
+    }
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
     for (int t0 = 0; t0 < S.ntri; t0 += 32) {
       int t = t0 + lane;
@@ -1701,3 +1747,97 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
 }
 
 }  // namespace dm
+
+namespace dm {
+// Debug aid (not part of the public ABI): run exhaustive face queries on the
+// grid of the last dm_delaunay call.  faces: int32[m][3] (p, a, b) device;
+// out: int32[m] winner (or -1).
+__global__ void k_debug_gq(DTArgs A, const int32_t *faces, int m, int32_t *out) {
+  const int lane = threadIdx.x & 31;
+  const GridParams g = *A.gp;
+  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= m) return;
+  int ovf = 0;
+  dmp::ExactScratch WS;
+  int r = A.dim == 3 ? gq3(A, g, faces[3 * w], faces[3 * w + 1], faces[3 * w + 2], lane, ovf, &WS)
+                     : gq2(A, g, faces[3 * w], faces[3 * w + 1], faces[3 * w + 2], lane, ovf, &WS);
+  if (lane == 0) out[w] = r;
+}
+}  // namespace dm
+
+extern "C" int dmdbg_face_query(int32_t dim, const float *pts, int64_t n,
+                                void *ws, size_t ws_bytes, const int32_t *faces,
+                                int32_t m, int32_t *out, void *stream) {
+  using namespace dm;
+  Carve c(ws, ws_bytes);
+  DTArgs a;
+  carve_dt(c, a, dim, n);
+  a.dim = dim;
+  a.n = n;
+  a.P = pts;
+  k_debug_gq<<<(m + 3) / 4, 128, 0, (cudaStream_t)stream>>>(a, faces, m, out);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+namespace dm {
+// Debug aid: device evaluation of orient3 (kind 0) / insph3_sos (kind 1) /
+// the float orient filter alone (kind 2) on index tuples int32[m][5].
+__global__ void k_debug_pred(const float *P, const int32_t *tup, int m, int kind,
+                             int32_t *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  float x[5][3];
+  for (int k = 0; k < 5; ++k) load_pt<3>(P, tup[5 * i + k], x[k]);
+  int ovf = 0;
+  dmp::ExactScratch WS;
+  if (kind == 0) {
+    out[i] = dmp::orient3(x[0], x[1], x[2], x[3], &WS);
+  } else if (kind == 1) {
+    out[i] = dmp::insph3_sos(x[0], x[1], x[2], x[3], x[4], &ovf, &WS);
+  } else if (kind == 2) {
+    float V[3], U[3], Y[3];
+    for (int k = 0; k < 3; ++k) {
+      V[k] = x[1][k] - x[0][k];
+      U[k] = x[2][k] - x[0][k];
+      Y[k] = x[3][k] - x[0][k];
+    }
+    out[i] = dmp::orient3_rel_filter<float>(V[0], V[1], V[2], U[0], U[1], U[2],
+                                            Y[0], Y[1], Y[2], 16.0f * DMP_U32);
+  } else if (kind == 3) {
+    out[i] = dmp::orient3_slow(x[0], x[1], x[2], x[3], &WS);
+  } else {
+    out[i] = dmp::orient3_exact(x[0], x[1], x[2], x[3], &WS);
+  }
+}
+}  // namespace dm
+
+extern "C" int dmdbg_predicates(const float *pts, const int32_t *tup, int32_t m,
+                                int32_t kind, int32_t *out, void *stream) {
+  dm::k_debug_pred<<<(m + 127) / 128, 128, 0, (cudaStream_t)stream>>>(pts, tup, m, kind, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+namespace dm {
+// Debug aid: FP64 rounding behaviour of the device (op 0 add, 1 mul, 2 fma,
+// 3 two_sum tail, 4 two_prod tail).
+__global__ void k_debug_fp64(const double *a, const double *b, const double *c,
+                             int m, int op, double *out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double x, y;
+  switch (op) {
+    case 0: out[i] = __dadd_rn(a[i], b[i]); break;
+    case 1: out[i] = __dmul_rn(a[i], b[i]); break;
+    case 2: out[i] = fma(a[i], b[i], c[i]); break;
+    case 3: dmp::two_sum(a[i], b[i], x, y); out[i] = y; break;
+    case 4: dmp::two_prod(a[i], b[i], x, y); out[i] = y; break;
+    case 5: out[i] = a[i] - b[i]; break;
+  }
+}
+}  // namespace dm
+extern "C" int dmdbg_fp64(const double *a, const double *b, const double *c,
+                          int32_t m, int32_t op, double *out, void *stream) {
+  dm::k_debug_fp64<<<(m + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, m, op, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}

@@ -36,6 +36,11 @@
 
 #if defined(__CUDACC__)
 #define DM_HD __host__ __device__ __forceinline__
+// The exact stages are out-of-line functions that keep every expansion in a
+// caller-provided ExactScratch (allocated once in the kernel's own frame).
+// Out-of-line device functions that owned local arrays computed wrong
+// results with nvcc 13.0 for sm_103a; the scratch form is exact and keeps a
+// single copy of each stage per translation unit.
 #define DM_HD_NI static __host__ __device__ __noinline__
 #else
 #define DM_HD static inline
@@ -44,23 +49,37 @@
 
 namespace dmp {
 
+// Every operation of the error-free transformations must round on its own:
+// a multiply fused into a following add (FMA contraction, nvcc's default)
+// breaks Two-Sum.  Device code uses the explicitly rounded intrinsics, which
+// are never contracted; host code is compiled with -ffp-contract=off.
+#if defined(__CUDA_ARCH__)
+#define DMP_MUL(a, b) __dmul_rn((a), (b))
+#define DMP_ADD(a, b) __dadd_rn((a), (b))
+#define DMP_SUB(a, b) __dsub_rn((a), (b))
+#else
+#define DMP_MUL(a, b) ((a) * (b))
+#define DMP_ADD(a, b) ((a) + (b))
+#define DMP_SUB(a, b) ((a) - (b))
+#endif
+
 // ---------------------------------------------------------------------------
 // Error-free transformations (round-to-nearest-even FP64 arithmetic).
 DM_HD void two_sum(double a, double b, double &x, double &y) {
-  x = a + b;
-  double bv = x - a;
-  double av = x - bv;
-  double br = b - bv;
-  double ar = a - av;
-  y = ar + br;
+  x = DMP_ADD(a, b);
+  double bv = DMP_SUB(x, a);
+  double av = DMP_SUB(x, bv);
+  double br = DMP_SUB(b, bv);
+  double ar = DMP_SUB(a, av);
+  y = DMP_ADD(ar, br);
 }
 DM_HD void fast_two_sum(double a, double b, double &x, double &y) {
-  x = a + b;
-  double bv = x - a;
-  y = b - bv;
+  x = DMP_ADD(a, b);
+  double bv = DMP_SUB(x, a);
+  y = DMP_SUB(b, bv);
 }
 DM_HD void two_prod(double a, double b, double &x, double &y) {
-  x = a * b;
+  x = DMP_MUL(a, b);
   y = fma(a, b, -x);
 }
 
@@ -164,8 +183,8 @@ DM_HD void negate(int n, double *e) {
 // Exact predicates on raw FP32 coordinates.
 // xy-minor m(X,Y) = X_x Y_y - Y_x X_y as an expansion of <= 2 terms.
 DM_HD int minor2(const float *X, const float *Y, double *m) {
-  double p = (double)X[0] * (double)Y[1];  // exact: float*float
-  double q = (double)Y[0] * (double)X[1];
+  double p = DMP_MUL((double)X[0], (double)Y[1]);  // exact: float*float
+  double q = DMP_MUL((double)Y[0], (double)X[1]);
   double hi, lo;
   two_sum(p, -q, hi, lo);
   int n = 0;
@@ -174,11 +193,13 @@ DM_HD int minor2(const float *X, const float *Y, double *m) {
   return n;
 }
 
-// det3 of raw rows [A;B;C] (<= 12 terms), given its three xy-minors.
+// det3 of raw rows [A;B;C] (<= 12 terms), given its three xy-minors;
+// t (>= 20 doubles) is scratch.
 DM_HD int det3_from_minors(const float *A, const float *B, const float *C,
                            const double *mBC, int nBC, const double *mAC,
-                           int nAC, const double *mAB, int nAB, double *out) {
-  double t1[4], t2[4], t3[4], s12[8];
+                           int nAC, const double *mAB, int nAB, double *out,
+                           double *t) {
+  double *t1 = t, *t2 = t + 4, *t3 = t + 8, *s12 = t + 12;
   int n1 = scale_expansion(nBC, mBC, (double)A[2], t1);
   int n2 = scale_expansion(nAC, mAC, -(double)B[2], t2);
   int n3 = scale_expansion(nAB, mAB, (double)C[2], t3);
@@ -186,44 +207,80 @@ DM_HD int det3_from_minors(const float *A, const float *B, const float *C,
   return expansion_sum(n12, s12, n3, t3, out);
 }
 
+DM_HD int lex_greater(const float *p, const float *q, int dim) {
+  for (int i = 0; i < dim; ++i) {
+    if (p[i] > q[i]) return 1;
+    if (p[i] < q[i]) return 0;
+  }
+  return 0;
+}
+
+// point r of (a, b, c, d, e) without a local pointer array
+DM_HD const float *sel5(int r, const float *a, const float *b, const float *c,
+                        const float *d, const float *e) {
+  return r == 0 ? a : r == 1 ? b : r == 2 ? c : r == 3 ? d : e;
+}
+// rank of pair (i < j) among pairs of n items, enumerated i-major
+DM_HD int pair_index(int i, int j, int n) { return i * (2 * n - i - 1) / 2 + (j - i - 1); }
+// rank of triple (i < j < k) among triples of 5 items, enumerated i-major
+DM_HD int triple_index5(int i, int j, int k) {
+  int base = i == 0 ? 0 : i == 1 ? 6 : i == 2 ? 9 : 10;
+  int m = 4 - i, jj = j - i - 1, kk = k - i - 1;
+  return base + jj * (2 * m - jj - 1) / 2 + (kk - jj - 1);
+}
+
+// Work space of the exact stages (about 4.6 KB).
+#define DMP_ACC_CAP 112
+struct ExactScratch {
+  double m[10][2];
+  int nm[10];
+  double D3[10][12];
+  int nD3[10];
+  double o1[24], o2[24], o[48], tneg[12];
+  double acc[DMP_ACC_CAP], tmp[DMP_ACC_CAP], tmp2[DMP_ACC_CAP];
+  double w[3];
+  double e2[2];
+  double d3tmp[20];
+};
+
 // orient3(a,b,c,d) = det3(b,c,d) - det3(a,c,d) + det3(a,b,d) - det3(a,b,c)
 // (Laplace expansion of det[[x y z 1]] along the ones column).
 DM_HD_NI int orient3_exact(const float *a, const float *b, const float *c,
-                           const float *d) {
-  double mab[2], mac[2], mad[2], mbc[2], mbd[2], mcd[2];
-  int nab = minor2(a, b, mab), nac = minor2(a, c, mac), nad = minor2(a, d, mad);
-  int nbc = minor2(b, c, mbc), nbd = minor2(b, d, mbd), ncd = minor2(c, d, mcd);
-  double bcd[12], acd[12], abd[12], abc[12];
-  int n_bcd = det3_from_minors(b, c, d, mcd, ncd, mbd, nbd, mbc, nbc, bcd);
-  int n_acd = det3_from_minors(a, c, d, mcd, ncd, mad, nad, mac, nac, acd);
-  int n_abd = det3_from_minors(a, b, d, mbd, nbd, mad, nad, mab, nab, abd);
-  int n_abc = det3_from_minors(a, b, c, mbc, nbc, mac, nac, mab, nab, abc);
+                           const float *d, ExactScratch *W) {
+  double(*m)[2] = W->m;  // pairs ab ac ad bc bd cd
+  int nab = minor2(a, b, m[0]), nac = minor2(a, c, m[1]), nad = minor2(a, d, m[2]);
+  int nbc = minor2(b, c, m[3]), nbd = minor2(b, d, m[4]), ncd = minor2(c, d, m[5]);
+  double *bcd = W->D3[0], *acd = W->D3[1], *abd = W->D3[2], *abc = W->D3[3];
+  int n_bcd = det3_from_minors(b, c, d, m[5], ncd, m[4], nbd, m[3], nbc, bcd, W->d3tmp);
+  int n_acd = det3_from_minors(a, c, d, m[5], ncd, m[2], nad, m[1], nac, acd, W->d3tmp);
+  int n_abd = det3_from_minors(a, b, d, m[4], nbd, m[2], nad, m[0], nab, abd, W->d3tmp);
+  int n_abc = det3_from_minors(a, b, c, m[3], nbc, m[1], nac, m[0], nab, abc, W->d3tmp);
   negate(n_acd, acd);
   negate(n_abc, abc);
-  double s1[24], s2[24], s[48];
-  int k1 = expansion_sum(n_bcd, bcd, n_acd, acd, s1);
-  int k2 = expansion_sum(n_abd, abd, n_abc, abc, s2);
-  int k = expansion_sum(k1, s1, k2, s2, s);
-  k = compress(k, s);
-  return expansion_sign(k, s);
+  int k1 = expansion_sum(n_bcd, bcd, n_acd, acd, W->o1);
+  int k2 = expansion_sum(n_abd, abd, n_abc, abc, W->o2);
+  int k = expansion_sum(k1, W->o1, k2, W->o2, W->o);
+  k = compress(k, W->o);
+  return expansion_sign(k, W->o);
 }
 
 // orient2(a,b,c) = m(b,c) - m(a,c) + m(a,b)
-DM_HD_NI int orient2_exact(const float *a, const float *b, const float *c) {
-  double mbc[2], mac[2], mab[2], s1[4], s[6];
+DM_HD_NI int orient2_exact(const float *a, const float *b, const float *c,
+                           ExactScratch *W) {
+  double *mbc = W->m[0], *mac = W->m[1], *mab = W->m[2];
   int nbc = minor2(b, c, mbc), nac = minor2(a, c, mac), nab = minor2(a, b, mab);
   negate(nac, mac);
-  int k1 = expansion_sum(nbc, mbc, nac, mac, s1);
-  int k = expansion_sum(k1, s1, nab, mab, s);
-  k = compress(k, s);
-  return expansion_sign(k, s);
+  int k1 = expansion_sum(nbc, mbc, nac, mac, W->o1);
+  int k = expansion_sum(k1, W->o1, nab, mab, W->o);
+  k = compress(k, W->o);
+  return expansion_sign(k, W->o);
 }
 
-// exact lifted coordinate x^2 + y^2 (+ z^2) as an expansion (<= 3 terms)
-DM_HD int lift_exact(const float *X, int dim, double *w) {
-  double x2 = (double)X[0] * (double)X[0];
-  double y2 = (double)X[1] * (double)X[1];
-  double e[2];
+// exact lifted coordinate x^2 + y^2 (+ z^2) as an expansion (<= 3 terms);
+// e (2 doubles) is scratch.
+DM_HD int lift_exact(const float *X, int dim, double *w, double *e) {
+  double x2 = DMP_MUL((double)X[0], (double)X[0]);
+  double y2 = DMP_MUL((double)X[1], (double)X[1]);
   double hi, lo;
   two_sum(x2, y2, hi, lo);
   int n = 0;
@@ -233,13 +290,12 @@ DM_HD int lift_exact(const float *X, int dim, double *w) {
     for (int i = 0; i < n; ++i) w[i] = e[i];
     return n;
   }
-  double z2 = (double)X[2] * (double)X[2];
+  double z2 = DMP_MUL((double)X[2], (double)X[2]);
   return grow_expansion(n, e, z2, w);
 }
 
 // accumulate acc += coef * w  (coef, w expansions); acc kept compressed.
 // Returns new accumulator length, or -1 when a capacity would overflow.
-#define DMP_ACC_CAP 192
 DM_HD int acc_add_product(int nacc, double *acc, int ncoef, const double *coef,
                           int nw, const double *w, double *tmp, double *tmp2) {
   for (int j = 0; j < nw; ++j) {
@@ -258,101 +314,76 @@ DM_HD int acc_add_product(int nacc, double *acc, int ncoef, const double *coef,
 // Returns the sign; *overflow set to 1 if an expansion would exceed its
 // capacity (never happens for finite FP32 inputs of realistic range).
 DM_HD_NI int insph3_exact(const float *a, const float *b, const float *c,
-                          const float *d, const float *e, int *overflow) {
-  const float *P[5] = {a, b, c, d, e};
-  // 10 xy-minors m[i][j], i<j
-  double m[10][2];
-  int nm[10];
-  int idx[5][5];
-  int t = 0;
+                          const float *d, const float *e, int *overflow,
+                          ExactScratch *W) {
   for (int i = 0; i < 5; ++i)
     for (int j = i + 1; j < 5; ++j) {
-      idx[i][j] = t;
-      nm[t] = minor2(P[i], P[j], m[t]);
-      ++t;
+      int t = pair_index(i, j, 5);
+      W->nm[t] = minor2(sel5(i, a, b, c, d, e), sel5(j, a, b, c, d, e), W->m[t]);
     }
-  // 10 det3 over triples i<j<k, compressed (<= 12 terms each)
-  double D3[10][12];
-  int nD3[10];
-  int tid[5][5][5];
-  t = 0;
   for (int i = 0; i < 5; ++i)
     for (int j = i + 1; j < 5; ++j)
       for (int k = j + 1; k < 5; ++k) {
-        tid[i][j][k] = t;
-        int mjk = idx[j][k], mik = idx[i][k], mij = idx[i][j];
-        nD3[t] = det3_from_minors(P[i], P[j], P[k], m[mjk], nm[mjk], m[mik],
-                                  nm[mik], m[mij], nm[mij], D3[t]);
-        nD3[t] = compress(nD3[t], D3[t]);
-        ++t;
+        int t = triple_index5(i, j, k);
+        int mjk = pair_index(j, k, 5), mik = pair_index(i, k, 5), mij = pair_index(i, j, 5);
+        W->nD3[t] = det3_from_minors(sel5(i, a, b, c, d, e), sel5(j, a, b, c, d, e),
+                                     sel5(k, a, b, c, d, e), W->m[mjk], W->nm[mjk],
+                                     W->m[mik], W->nm[mik], W->m[mij], W->nm[mij], W->D3[t],
+                                     W->d3tmp);
+        W->nD3[t] = compress(W->nD3[t], W->D3[t]);
       }
-  double acc[DMP_ACC_CAP], tmp[DMP_ACC_CAP], tmp2[DMP_ACC_CAP];
-  int nacc = 0;
-  acc[0] = 0.0;
-  nacc = 1;
+  W->acc[0] = 0.0;
+  int nacc = 1;
   for (int r = 0; r < 5; ++r) {
-    // orient of the other four points (q0<q1<q2<q3 in argument order)
-    int q[4], nq = 0;
-    for (int s = 0; s < 5; ++s)
-      if (s != r) q[nq++] = s;
+    // the other four points in argument order
+    int q0 = 0 + (0 >= r), q1 = 1 + (1 >= r), q2 = 2 + (2 >= r), q3 = 3 + (3 >= r);
     // o(q0,q1,q2,q3) = det3(q1q2q3) - det3(q0q2q3) + det3(q0q1q3) - det3(q0q1q2)
-    double o1[24], o2[24], o[48], tneg[12];
-    int t0 = tid[q[1]][q[2]][q[3]], t1 = tid[q[0]][q[2]][q[3]];
-    int t2 = tid[q[0]][q[1]][q[3]], t3 = tid[q[0]][q[1]][q[2]];
-    for (int i = 0; i < nD3[t1]; ++i) tneg[i] = -D3[t1][i];
-    int k1 = expansion_sum(nD3[t0], D3[t0], nD3[t1], tneg, o1);
-    for (int i = 0; i < nD3[t3]; ++i) tneg[i] = -D3[t3][i];
-    int k2 = expansion_sum(nD3[t2], D3[t2], nD3[t3], tneg, o2);
-    int ko = expansion_sum(k1, o1, k2, o2, o);
-    ko = compress(ko, o);
-    if ((r & 1) == 1) negate(ko, o);  // alternating signs: +a -b +c -d +e
-    double w[3];
-    int nw = lift_exact(P[r], 3, w);
-    nacc = acc_add_product(nacc, acc, ko, o, nw, w, tmp, tmp2);
+    int t0 = triple_index5(q1, q2, q3), t1 = triple_index5(q0, q2, q3);
+    int t2 = triple_index5(q0, q1, q3), t3 = triple_index5(q0, q1, q2);
+    for (int i = 0; i < W->nD3[t1]; ++i) W->tneg[i] = -W->D3[t1][i];
+    int k1 = expansion_sum(W->nD3[t0], W->D3[t0], W->nD3[t1], W->tneg, W->o1);
+    for (int i = 0; i < W->nD3[t3]; ++i) W->tneg[i] = -W->D3[t3][i];
+    int k2 = expansion_sum(W->nD3[t2], W->D3[t2], W->nD3[t3], W->tneg, W->o2);
+    int ko = expansion_sum(k1, W->o1, k2, W->o2, W->o);
+    ko = compress(ko, W->o);
+    if ((r & 1) == 1) negate(ko, W->o);  // alternating signs: +a -b +c -d +e
+    int nw = lift_exact(sel5(r, a, b, c, d, e), 3, W->w, W->e2);
+    nacc = acc_add_product(nacc, W->acc, ko, W->o, nw, W->w, W->tmp, W->tmp2);
     if (nacc < 0) {
       *overflow = 1;
       return 0;
     }
   }
-  return expansion_sign(nacc, acc);
+  return expansion_sign(nacc, W->acc);
 }
 
 // incirc2(a,b,c,d) = -w_a o(b,c,d) + w_b o(a,c,d) - w_c o(a,b,d) + w_d o(a,b,c)
 DM_HD_NI int incirc2_exact(const float *a, const float *b, const float *c,
-                           const float *d, int *overflow) {
-  const float *P[4] = {a, b, c, d};
-  double m[6][2];
-  int nm[6], idx[4][4], t = 0;
+                           const float *d, int *overflow, ExactScratch *W) {
   for (int i = 0; i < 4; ++i)
     for (int j = i + 1; j < 4; ++j) {
-      idx[i][j] = t;
-      nm[t] = minor2(P[i], P[j], m[t]);
-      ++t;
+      int t = pair_index(i, j, 4);
+      W->nm[t] = minor2(sel5(i, a, b, c, d, d), sel5(j, a, b, c, d, d), W->m[t]);
     }
-  double acc[DMP_ACC_CAP], tmp[DMP_ACC_CAP], tmp2[DMP_ACC_CAP];
+  W->acc[0] = 0.0;
   int nacc = 1;
-  acc[0] = 0.0;
   for (int r = 0; r < 4; ++r) {
-    int q[3], nq = 0;
-    for (int s = 0; s < 4; ++s)
-      if (s != r) q[nq++] = s;
+    int q0 = 0 + (0 >= r), q1 = 1 + (1 >= r), q2 = 2 + (2 >= r);
     // o(q0,q1,q2) = m(q1,q2) - m(q0,q2) + m(q0,q1)
-    double neg[2], s1[4], o[6];
-    int a12 = idx[q[1]][q[2]], a02 = idx[q[0]][q[2]], a01 = idx[q[0]][q[1]];
-    for (int i = 0; i < nm[a02]; ++i) neg[i] = -m[a02][i];
-    int k1 = expansion_sum(nm[a12], m[a12], nm[a02], neg, s1);
-    int ko = expansion_sum(k1, s1, nm[a01], m[a01], o);
-    ko = compress(ko, o);
-    if ((r & 1) == 0) negate(ko, o);  // -a +b -c +d
-    double w[3];
-    int nw = lift_exact(P[r], 2, w);
-    nacc = acc_add_product(nacc, acc, ko, o, nw, w, tmp, tmp2);
+    int a12 = pair_index(q1, q2, 4), a02 = pair_index(q0, q2, 4), a01 = pair_index(q0, q1, 4);
+    for (int i = 0; i < W->nm[a02]; ++i) W->tneg[i] = -W->m[a02][i];
+    int k1 = expansion_sum(W->nm[a12], W->m[a12], W->nm[a02], W->tneg, W->o1);
+    int ko = expansion_sum(k1, W->o1, W->nm[a01], W->m[a01], W->o);
+    ko = compress(ko, W->o);
+    if ((r & 1) == 0) negate(ko, W->o);  // -a +b -c +d
+    int nw = lift_exact(sel5(r, a, b, c, d, d), 2, W->w, W->e2);
+    nacc = acc_add_product(nacc, W->acc, ko, W->o, nw, W->w, W->tmp, W->tmp2);
     if (nacc < 0) {
       *overflow = 1;
       return 0;
     }
   }
-  return expansion_sign(nacc, acc);
+  return expansion_sign(nacc, W->acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -455,8 +486,8 @@ DM_HD int exact_diff(const float *b, const float *a, int dim, double *out) {
 
 // ---------------------------------------------------------------------------
 // Full predicates on raw coordinates (FP64 filter then exact).
-DM_HD_NI int orient3_slow(const float *a, const float *b, const float *c,
-                          const float *d) {
+DM_HD int orient3_slow(const float *a, const float *b, const float *c,
+                          const float *d, ExactScratch *W) {
   double X[3], Y[3], Z[3];
   if (exact_diff(b, a, 3, X) && exact_diff(c, a, 3, Y) && exact_diff(d, a, 3, Z)) {
     int s = orient3_rel_filter<double>(X[0], X[1], X[2], Y[0], Y[1], Y[2], Z[0],
@@ -467,83 +498,79 @@ DM_HD_NI int orient3_slow(const float *a, const float *b, const float *c,
          (Z[0] == 0 && Z[1] == 0 && Z[2] == 0)))
       return 0;
   }
-  return orient3_exact(a, b, c, d);
+  return orient3_exact(a, b, c, d, W);
 }
 
 DM_HD int orient3(const float *a, const float *b, const float *c,
-                  const float *d) {
+                  const float *d, ExactScratch *W) {
   float X[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
   float Y[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
   float Z[3] = {d[0] - a[0], d[1] - a[1], d[2] - a[2]};
   int s = orient3_rel_filter<float>(X[0], X[1], X[2], Y[0], Y[1], Y[2], Z[0],
                                     Z[1], Z[2], 16.0f * DMP_U32);
   if (s) return s;
-  return orient3_slow(a, b, c, d);
+  return orient3_slow(a, b, c, d, W);
 }
 
-DM_HD_NI int orient2_slow(const float *a, const float *b, const float *c) {
+DM_HD int orient2_slow(const float *a, const float *b, const float *c,
+                          ExactScratch *W) {
   double X[2], Y[2];
   if (exact_diff(b, a, 2, X) && exact_diff(c, a, 2, Y)) {
     int s = orient2_rel_filter<double>(X[0], X[1], Y[0], Y[1], 8.0 * DMP_U64);
     if (s) return s;
   }
-  return orient2_exact(a, b, c);
+  return orient2_exact(a, b, c, W);
 }
 
-DM_HD int orient2(const float *a, const float *b, const float *c) {
+DM_HD int orient2(const float *a, const float *b, const float *c,
+                  ExactScratch *W) {
   float X[2] = {b[0] - a[0], b[1] - a[1]};
   float Y[2] = {c[0] - a[0], c[1] - a[1]};
   int s = orient2_rel_filter<float>(X[0], X[1], Y[0], Y[1], 8.0f * DMP_U32);
   if (s) return s;
-  return orient2_slow(a, b, c);
+  return orient2_slow(a, b, c, W);
 }
 
-DM_HD int lex_greater(const float *p, const float *q, int dim) {
-  for (int i = 0; i < dim; ++i) {
-    if (p[i] > q[i]) return 1;
-    if (p[i] < q[i]) return 0;
-  }
-  return 0;
-}
 
 // unperturbed sign of insph3 (FP64 filter, then exact)
-DM_HD_NI int insph3_slow(const float *a, const float *b, const float *c,
-                         const float *d, const float *e, int *overflow) {
-  double X[3], Y[3], Z[3], W[3];
+DM_HD int insph3_slow(const float *a, const float *b, const float *c,
+                         const float *d, const float *e, int *overflow,
+                         ExactScratch *W) {
+  double X[3], Y[3], Z[3], Q[3];
   if (exact_diff(b, a, 3, X) && exact_diff(c, a, 3, Y) && exact_diff(d, a, 3, Z) &&
-      exact_diff(e, a, 3, W)) {
+      exact_diff(e, a, 3, Q)) {
     double wx = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
     double wy = Y[0] * Y[0] + Y[1] * Y[1] + Y[2] * Y[2];
     double wz = Z[0] * Z[0] + Z[1] * Z[1] + Z[2] * Z[2];
-    double ww = W[0] * W[0] + W[1] * W[1] + W[2] * W[2];
-    int s = insph3_rel_filter<double>(X, Y, Z, W, wx, wy, wz, ww, 48.0 * DMP_U64);
+    double ww = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2];
+    int s = insph3_rel_filter<double>(X, Y, Z, Q, wx, wy, wz, ww, 48.0 * DMP_U64);
     if (s) return s;
   }
-  return insph3_exact(a, b, c, d, e, overflow);
+  return insph3_exact(a, b, c, d, e, overflow, W);
 }
 
-// perturbed insph3: never 0 unless all five points are coplanar (or overflow)
-DM_HD_NI int insph3_sos_tail(const float *a, const float *b, const float *c,
-                             const float *d, const float *e) {
-  const float *P[5] = {a, b, c, d, e};
-  int ord[5] = {0, 1, 2, 3, 4};
-  // insertion sort, lexicographically descending
-  for (int i = 1; i < 5; ++i) {
-    int k = ord[i], j = i - 1;
-    while (j >= 0 && lex_greater(P[k], P[ord[j]], 3)) {
-      ord[j + 1] = ord[j];
-      --j;
+// perturbed insph3: never 0 unless all five points are coplanar (or overflow).
+// The coefficient of the lifted coordinate of point X (translated form):
+//   e: +o(a,b,c,d)  d: -o(a,b,c,e)  c: +o(a,b,d,e)  b: -o(a,c,d,e)  a: +o(b,c,d,e)
+// Points are visited from the lexicographically largest (largest
+// perturbation) down; the first non-zero coefficient decides.
+DM_HD int insph3_sos_tail(const float *a, const float *b, const float *c,
+                          const float *d, const float *e, ExactScratch *W) {
+  int done = 0;  // bit mask of visited points
+  for (int step = 0; step < 5; ++step) {
+    int best = -1;
+    for (int r = 0; r < 5; ++r) {
+      if (done >> r & 1) continue;
+      if (best < 0 || lex_greater(sel5(r, a, b, c, d, e), sel5(best, a, b, c, d, e), 3)) best = r;
     }
-    ord[j + 1] = k;
-  }
-  for (int i = 0; i < 5; ++i) {
+    done |= 1 << best;
     int s = 0;
-    switch (ord[i]) {
-      case 4: s = orient3(a, b, c, d); break;
-      case 3: s = -orient3(a, b, c, e); break;
-      case 2: s = orient3(a, b, d, e); break;
-      case 1: s = -orient3(a, c, d, e); break;
-      case 0: s = orient3(b, c, d, e); break;
+    switch (best) {
+      case 4: s = orient3(a, b, c, d, W); break;
+      case 3: s = -orient3(a, b, c, e, W); break;
+      case 2: s = orient3(a, b, d, e, W); break;
+      case 1: s = -orient3(a, c, d, e, W); break;
+      case 0: s = orient3(b, c, d, e, W); break;
     }
     if (s) return s;
   }
@@ -551,24 +578,25 @@ DM_HD_NI int insph3_sos_tail(const float *a, const float *b, const float *c,
 }
 
 DM_HD int insph3_sos(const float *a, const float *b, const float *c,
-                     const float *d, const float *e, int *overflow) {
+                     const float *d, const float *e, int *overflow,
+                     ExactScratch *W) {
   float X[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
   float Y[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
   float Z[3] = {d[0] - a[0], d[1] - a[1], d[2] - a[2]};
-  float W[3] = {e[0] - a[0], e[1] - a[1], e[2] - a[2]};
+  float Q[3] = {e[0] - a[0], e[1] - a[1], e[2] - a[2]};
   float wx = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
   float wy = Y[0] * Y[0] + Y[1] * Y[1] + Y[2] * Y[2];
   float wz = Z[0] * Z[0] + Z[1] * Z[1] + Z[2] * Z[2];
-  float ww = W[0] * W[0] + W[1] * W[1] + W[2] * W[2];
-  int s = insph3_rel_filter<float>(X, Y, Z, W, wx, wy, wz, ww, 48.0f * DMP_U32);
+  float ww = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2];
+  int s = insph3_rel_filter<float>(X, Y, Z, Q, wx, wy, wz, ww, 48.0f * DMP_U32);
   if (s) return s;
-  s = insph3_slow(a, b, c, d, e, overflow);
+  s = insph3_slow(a, b, c, d, e, overflow, W);
   if (s) return s;
-  return insph3_sos_tail(a, b, c, d, e);
+  return insph3_sos_tail(a, b, c, d, e, W);
 }
 
-DM_HD_NI int incirc2_slow(const float *a, const float *b, const float *c,
-                          const float *d, int *overflow) {
+DM_HD int incirc2_slow(const float *a, const float *b, const float *c,
+                          const float *d, int *overflow, ExactScratch *W) {
   double X[2], Y[2], Z[2];
   if (exact_diff(b, a, 2, X) && exact_diff(c, a, 2, Y) && exact_diff(d, a, 2, Z)) {
     double wx = X[0] * X[0] + X[1] * X[1];
@@ -577,30 +605,27 @@ DM_HD_NI int incirc2_slow(const float *a, const float *b, const float *c,
     int s = incirc2_rel_filter<double>(X, Y, Z, wx, wy, wz, 16.0 * DMP_U64);
     if (s) return s;
   }
-  return incirc2_exact(a, b, c, d, overflow);
+  return incirc2_exact(a, b, c, d, overflow, W);
 }
 
 // perturbation coefficients of incirc2 (translated form):
 //   d: +o(a,b,c)  c: -o(a,b,d)  b: +o(a,c,d)  a: -o(b,c,d)
-DM_HD_NI int incirc2_sos_tail(const float *a, const float *b, const float *c,
-                              const float *d) {
-  const float *P[4] = {a, b, c, d};
-  int ord[4] = {0, 1, 2, 3};
-  for (int i = 1; i < 4; ++i) {
-    int k = ord[i], j = i - 1;
-    while (j >= 0 && lex_greater(P[k], P[ord[j]], 2)) {
-      ord[j + 1] = ord[j];
-      --j;
+DM_HD int incirc2_sos_tail(const float *a, const float *b, const float *c,
+                           const float *d, ExactScratch *W) {
+  int done = 0;
+  for (int step = 0; step < 4; ++step) {
+    int best = -1;
+    for (int r = 0; r < 4; ++r) {
+      if (done >> r & 1) continue;
+      if (best < 0 || lex_greater(sel5(r, a, b, c, d, d), sel5(best, a, b, c, d, d), 2)) best = r;
     }
-    ord[j + 1] = k;
-  }
-  for (int i = 0; i < 4; ++i) {
+    done |= 1 << best;
     int s = 0;
-    switch (ord[i]) {
-      case 3: s = orient2(a, b, c); break;
-      case 2: s = -orient2(a, b, d); break;
-      case 1: s = orient2(a, c, d); break;
-      case 0: s = -orient2(b, c, d); break;
+    switch (best) {
+      case 3: s = orient2(a, b, c, W); break;
+      case 2: s = -orient2(a, b, d, W); break;
+      case 1: s = orient2(a, c, d, W); break;
+      case 0: s = -orient2(b, c, d, W); break;
     }
     if (s) return s;
   }
@@ -608,7 +633,7 @@ DM_HD_NI int incirc2_sos_tail(const float *a, const float *b, const float *c,
 }
 
 DM_HD int incirc2_sos(const float *a, const float *b, const float *c,
-                      const float *d, int *overflow) {
+                      const float *d, int *overflow, ExactScratch *W) {
   float X[2] = {b[0] - a[0], b[1] - a[1]};
   float Y[2] = {c[0] - a[0], c[1] - a[1]};
   float Z[2] = {d[0] - a[0], d[1] - a[1]};
@@ -617,9 +642,9 @@ DM_HD int incirc2_sos(const float *a, const float *b, const float *c,
   float wz = Z[0] * Z[0] + Z[1] * Z[1];
   int s = incirc2_rel_filter<float>(X, Y, Z, wx, wy, wz, 16.0f * DMP_U32);
   if (s) return s;
-  s = incirc2_slow(a, b, c, d, overflow);
+  s = incirc2_slow(a, b, c, d, overflow, W);
   if (s) return s;
-  return incirc2_sos_tail(a, b, c, d);
+  return incirc2_sos_tail(a, b, c, d, W);
 }
 
 }  // namespace dmp
