@@ -1,0 +1,38 @@
+"""Builds the oracle's C restatement (test infrastructure) into oracle/lib/,
+and the reference's own C++ modules into oracle/_ref/ when the reference
+sources and pybind11 are available."""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "lib", "liboracle.so")
+
+
+def build_oracle_c():
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    src = os.path.join(HERE, "limgrad.c")
+    if os.path.exists(LIB) and os.path.getmtime(LIB) > os.path.getmtime(src):
+        return LIB
+    subprocess.run(["gcc", "-O2", "-shared", "-fPIC", "-ffp-contract=off", src, "-o", LIB, "-lm"], check=True)
+    return LIB
+
+
+def build_ref():
+    ref = os.environ.get("SEISMICMESH_REF", "/root/reference")
+    if not os.path.isdir(ref):
+        return None
+    try:
+        import pybind11  # noqa: F401
+    except ImportError:
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={ref}"], check=True)
+    return os.path.join(HERE, "_ref")
+
+
+def build_all():
+    build_oracle_c()
+    build_ref()
+
+
+if __name__ == "__main__":
+    build_all()

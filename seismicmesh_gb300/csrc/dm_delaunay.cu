@@ -65,6 +65,8 @@ struct DTArgs {
   int64_t cap_cells_out;
   int64_t *counters;
   int64_t cap_cells, cap_blocks;
+  int dbg_vertex;  // debug aid: level-1 state of this vertex goes to dbg
+  int32_t *dbg;
 };
 
 static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
@@ -477,73 +479,84 @@ __device__ __forceinline__ bool certified3(float4 A, float4 B, float4 C,
   return num2 <= lim * lim * det * det;
 }
 
+// Collect the candidate set Q of vertex p: every point within reff of p,
+// reff chosen so |Q| <= CAP.  The cells within K of p's cell are scanned; the
+// covered radius rcov is p's distance to the faces of that block (sides
+// clipped by the grid need no limit).  A 16-bin histogram of d / r picks the
+// largest radius whose ball holds <= CAP points; when the first bin alone
+// overflows (dense clusters) the radius is divided by 16 and re-histogrammed.
 template <int DIM>
 __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const GridParams &g,
-                          int ip, const float *px, int lane) {
-  constexpr int K = L1<DIM>::K, W = 2 * K + 1;
-  constexpr int NCELL = DIM == 3 ? W * W * W : W * W;
+                                          int ip, const float *px, int lane, int K) {
+  const int W = 2 * K + 1;
+  const int NCELL = DIM == 3 ? W * W * W : W * W;
   int cc[3];
   for (int k = 0; k < DIM; ++k) cc[k] = cell_coord(g, px[k], k);
-  // covered radius: distance from p to the faces of the block of cells
   float rcov = FLT_MAX;
   for (int k = 0; k < DIM; ++k) {
     if (cc[k] - K > 0) rcov = fminf(rcov, px[k] - (g.lo[k] + (cc[k] - K) * g.cs));
     if (cc[k] + K + 1 < g.dims[k])
       rcov = fminf(rcov, (g.lo[k] + (cc[k] + K + 1) * g.cs) - px[k]);
   }
+  // a block clipped on every side holds every point: any radius beyond the
+  // grid diagonal is covered
+  rcov = fminf(rcov, g.cs * (float)(g.dims[0] + g.dims[1] + g.dims[2] + 1));
   rcov = rcov * (1.f - 1e-5f);
-  if (rcov > 1e30f) rcov = 1e30f;
-  float rc2 = rcov * rcov;
-  // pass 1: count, with a 16-bin histogram of d / rcov
-  int bins[16];
+  float rcnt = rcov;
+  int bmax = -1;
+  for (int round = 0; round < 6 && bmax < 0; ++round, rcnt *= (1.f / 16.f)) {
+    const float rc2 = rcnt * rcnt;
+    int bins[16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) bins[k] = 0;
-  int total = 0;
-  for (int t = lane; t < NCELL; t += 32) {
-    int d0 = t % W - K, d1 = (t / W) % W - K, d2 = DIM == 3 ? t / (W * W) - K : 0;
-    int x = cc[0] + d0, y = cc[1] + d1, z = DIM == 3 ? cc[2] + d2 : 0;
-    if (x < 0 || y < 0 || z < 0 || x >= g.dims[0] || y >= g.dims[1] ||
-        (DIM == 3 && z >= g.dims[2]))
-      continue;
-    int c = x + g.dims[0] * (y + g.dims[1] * z);
-    for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) {
-      int q = A.sorted[i];
-      if (q == ip || A.dup[q]) continue;
-      float xq[3];
-      load_pt<DIM>(A.P, q, xq);
-      float d2s = 0.f;
-      for (int k = 0; k < DIM; ++k) {
-        float dd = xq[k] - px[k];
-        d2s += dd * dd;
-      }
-      if (d2s <= rc2) {
-        ++total;
-        int bidx = min(15, (int)(sqrtf(d2s) / rcov * 16.f));
-        for (int k = 0; k < 16; ++k) bins[k] += (k == bidx);
+    for (int k = 0; k < 16; ++k) bins[k] = 0;
+    int total = 0;
+    for (int t = lane; t < NCELL; t += 32) {
+      int d0 = t % W - K, d1 = (t / W) % W - K, d2 = DIM == 3 ? t / (W * W) - K : 0;
+      int x = cc[0] + d0, y = cc[1] + d1, z = DIM == 3 ? cc[2] + d2 : 0;
+      if (x < 0 || y < 0 || z < 0 || x >= g.dims[0] || y >= g.dims[1] ||
+          (DIM == 3 && z >= g.dims[2]))
+        continue;
+      int c = x + g.dims[0] * (y + g.dims[1] * z);
+      for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) {
+        int q = A.sorted[i];
+        if (q == ip || A.dup[q]) continue;
+        float xq[3];
+        load_pt<DIM>(A.P, q, xq);
+        float d2s = 0.f;
+        for (int k = 0; k < DIM; ++k) {
+          float dd = xq[k] - px[k];
+          d2s += dd * dd;
+        }
+        if (d2s <= rc2) {
+          ++total;
+          int bidx = min(15, (int)(sqrtf(d2s) / rcnt * 16.f));
+#pragma unroll
+          for (int k = 0; k < 16; ++k) bins[k] += (k == bidx);
+        }
       }
     }
-  }
-  for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
-  int bmax = 15;
-  float reff = rcov;
-  if (total > L1<DIM>::CAP) {
+    for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+    if (total <= L1<DIM>::CAP) {
+      bmax = 15;
+      break;
+    }
     int cum = 0;
-    bmax = -1;
     for (int k = 0; k < 16; ++k) {
       int v = bins[k];
       for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       cum += v;
       if (cum <= L1<DIM>::CAP) bmax = k;
     }
-    reff = rcov * (bmax + 1) / 16.f * (1.f - 1e-5f);
+    if (bmax >= 0) break;
   }
+  const float reff = bmax == 15 ? rcnt : rcnt * (bmax + 1) / 16.f * (1.f - 1e-5f);
   if (lane == 0) {
     S.nc = 0;
     S.reff = bmax < 0 ? 0.f : reff;
   }
   __syncwarp();
   if (bmax < 0) return;
-  // pass 2: collect
+  const float rc2 = rcnt * rcnt;
   for (int t = lane; t < NCELL; t += 32) {
     int d0 = t % W - K, d1 = (t / W) % W - K, d2 = DIM == 3 ? t / (W * W) - K : 0;
     int x = cc[0] + d0, y = cc[1] + d1, z = DIM == 3 ? cc[2] + d2 : 0;
@@ -562,7 +575,7 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
         d2s += r[k] * r[k];
       }
       if (d2s > rc2) continue;
-      int bidx = min(15, (int)(sqrtf(d2s) / rcov * 16.f));
+      int bidx = min(15, (int)(sqrtf(d2s) / rcnt * 16.f));
       if (bidx > bmax) continue;
       int slot = atomicAdd(&S.nc, 1);
       if (slot < L1<DIM>::CAP) {
@@ -576,6 +589,19 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
   __syncwarp();
   if (lane == 0 && S.nc > L1<DIM>::CAP) S.nc = L1<DIM>::CAP;  // cannot happen
   __syncwarp();
+}
+
+// is the cell (p, a, b, c) of a packed link triangle empty w.r.t. every
+// candidate?  (exact, warp-cooperative)
+__device__ __forceinline__ bool empty3L(const WarpL1<3> &S, const float *P, int ip,
+                                        uint32_t tr, int lane, int &ovf,
+                                        dmp::ExactScratch *W) {
+  int a = un0(tr), b = un1(tr), c = un2(tr);
+  bool inside = false;
+  for (int j = lane; j < S.nc; j += 32)
+    if (!inside && j != a && j != b && j != c)
+      inside = is3L(S, P, ip, a, b, c, j, ovf, W) < 0;
+  return !__any_sync(0xffffffffu, inside);
 }
 
 // seed search (3D): returns packed link triangle or 0xffffffff
@@ -635,12 +661,19 @@ __device__ __forceinline__ uint32_t seed3L(const WarpL1<3> &S, const float *P,
       pk2 = ck;
       pg2 = cg;
       int q2 = cj;
+      // the cell on one side of face (p, q1, q2) is accepted once no
+      // candidate lies inside its circumsphere (this also rejects faces with
+      // a coplanar point inside their circumcircle)
+      uint32_t cand;
       int xp = gw3L(S, P, ip, q1, q2, lane, ovf, W);
-      int xm = gw3L(S, P, ip, q2, q1, lane, ovf, W);
-      if (xp < 0 && xm < 0) continue;
-      bool ok = true;
-      if (xp >= 0 && xm >= 0) ok = is3L(S, P, ip, q1, q2, xp, xm, ovf, W) > 0;
-      if (ok) return xp >= 0 ? pack3(q1, q2, xp) : pack3(q2, q1, xm);
+      if (xp >= 0) {
+        cand = pack3(q1, q2, xp);
+      } else {
+        int xm = gw3L(S, P, ip, q2, q1, lane, ovf, W);
+        if (xm < 0) continue;
+        cand = pack3(q2, q1, xm);
+      }
+      if (empty3L(S, P, ip, cand, lane, ovf, W)) return cand;
     }
   }
   return 0xffffffffu;
@@ -763,12 +796,21 @@ __device__ __forceinline__ uint32_t seed2L(const WarpL1<2> &S, const float *P,
     pk = bk;
     pg = bg;
     int q1 = bj;
+    uint32_t cand;
     int xp = gw2L(S, P, ip, q1, +1, lane, ovf, W);
-    int xm = gw2L(S, P, ip, q1, -1, lane, ovf, W);
-    if (xp < 0 && xm < 0) continue;
-    bool ok = true;
-    if (xp >= 0 && xm >= 0) ok = ic2L(S, P, ip, q1, xp, xm, ovf, W) > 0;
-    if (ok) return xp >= 0 ? pack3(q1, xp, 0) : pack3(xm, q1, 0);
+    if (xp >= 0) {
+      cand = pack3(q1, xp, 0);
+    } else {
+      int xm = gw2L(S, P, ip, q1, -1, lane, ovf, W);
+      if (xm < 0) continue;
+      cand = pack3(xm, q1, 0);
+    }
+    // accept once no candidate lies inside the triangle's circumcircle
+    int a = un0(cand), b = un1(cand);
+    bool inside = false;
+    for (int j = lane; j < nc; j += 32)
+      if (!inside && j != a && j != b) inside = ic2L(S, P, ip, a, b, j, ovf, W) < 0;
+    if (!__any_sync(0xffffffffu, inside)) return cand;
   }
   return 0xffffffffu;
 }
@@ -797,7 +839,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
     if (A.dup[ip]) continue;
     float px[3];
     load_pt<3>(A.P, ip, px);
-    gather_l1<3>(S, A, g, ip, px, lane);
+    gather_l1<3>(S, A, g, ip, px, lane, L1<3>::K);
     int ovf = 0;
     uint32_t seed = S.nc >= 3 ? seed3L(S, A.P, ip, lane, ovf, W) : 0xffffffffu;
     if (seed == 0xffffffffu) {
@@ -852,6 +894,24 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
       }
       if (S.flags) break;
     }
+    if (ip == A.dbg_vertex && A.dbg) {
+      // [nc, ntri, hull, flags, reff bits, ids[nc]..., tri[ntri] (3 ids each)]
+      if (lane == 0) {
+        A.dbg[0] = S.nc;
+        A.dbg[1] = S.ntri;
+        A.dbg[2] = hull;
+        A.dbg[3] = S.flags;
+        A.dbg[4] = __float_as_int(S.reff);
+      }
+      for (int k = lane; k < S.nc; k += 32) A.dbg[8 + k] = S.id[k];
+      for (int t = lane; t < S.ntri; t += 32) {
+        uint32_t tr = S.tri[t];
+        A.dbg[8 + 128 + 3 * t] = S.id[un0(tr)];
+        A.dbg[8 + 128 + 3 * t + 1] = S.id[un1(tr)];
+        A.dbg[8 + 128 + 3 * t + 2] = S.id[un2(tr)];
+      }
+      __syncwarp();
+    }
     // certification
     bool allok = !hull && !S.flags;
     int cert_any = -1;
@@ -864,7 +924,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
     allok = __all_sync(0xffffffffu, allok);
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
     if (!allok) {
-      unsigned m = __ballot_sync(0xffffffffu, cert_any >= 0);
+      unsigned m = S.flags ? 0u : __ballot_sync(0xffffffffu, cert_any >= 0);
       int4 sd;
       if (m) {
         int t = __shfl_sync(0xffffffffu, cert_any, __ffs(m) - 1);
@@ -915,7 +975,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
     if (A.dup[ip]) continue;
     float px[2];
     load_pt<2>(A.P, ip, px);
-    gather_l1<2>(S, A, g, ip, px, lane);
+    gather_l1<2>(S, A, g, ip, px, lane, L1<2>::K);
     int ovf = 0;
     uint32_t seed = S.nc >= 2 ? seed2L(S, A.P, ip, lane, ovf, W) : 0xffffffffu;
     if (seed == 0xffffffffu) {
@@ -984,7 +1044,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS) k_star2_l1(DTArgs A) {
     allok = __all_sync(0xffffffffu, allok);
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
     if (!allok) {
-      unsigned m = __ballot_sync(0xffffffffu, cert_any >= 0);
+      unsigned m = S.flags ? 0u : __ballot_sync(0xffffffffu, cert_any >= 0);
       int4 sd;
       int t = m ? __shfl_sync(0xffffffffu, cert_any, __ffs(m) - 1) : 0;
       uint32_t tr = S.tri[t];
@@ -1418,6 +1478,283 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
   return tourney2(A, E, best, ovf, W);
 }
 
+// exact emptiness of a circumsphere (circle) over the whole point set: every
+// point in a cell that meets the ball is tested with the perturbed predicate.
+template <int DIM>
+__device__ __forceinline__ bool gempty(const DTArgs &A, const GridParams &g, int ip,
+                                       const int *v, int lane, int &ovf,
+                                       dmp::ExactScratch *W) {
+  float P0[3], X[3][3];
+  load_pt<DIM>(A.P, ip, P0);
+  for (int k = 0; k < DIM; ++k) load_pt<DIM>(A.P, v[k], X[k]);
+  double a[3][3];
+  for (int k = 0; k < DIM; ++k)
+    for (int j = 0; j < DIM; ++j) a[k][j] = (double)X[k][j] - P0[j];
+  double cen[3] = {0, 0, 0}, rad;
+  if (DIM == 3) {
+    double bc[3] = {a[1][1] * a[2][2] - a[1][2] * a[2][1], a[1][2] * a[2][0] - a[1][0] * a[2][2],
+                    a[1][0] * a[2][1] - a[1][1] * a[2][0]};
+    double ca[3] = {a[2][1] * a[0][2] - a[2][2] * a[0][1], a[2][2] * a[0][0] - a[2][0] * a[0][2],
+                    a[2][0] * a[0][1] - a[2][1] * a[0][0]};
+    double ab[3] = {a[0][1] * a[1][2] - a[0][2] * a[1][1], a[0][2] * a[1][0] - a[0][0] * a[1][2],
+                    a[0][0] * a[1][1] - a[0][1] * a[1][0]};
+    double det = a[0][0] * bc[0] + a[0][1] * bc[1] + a[0][2] * bc[2];
+    double l0 = a[0][0] * a[0][0] + a[0][1] * a[0][1] + a[0][2] * a[0][2];
+    double l1 = a[1][0] * a[1][0] + a[1][1] * a[1][1] + a[1][2] * a[1][2];
+    double l2 = a[2][0] * a[2][0] + a[2][1] * a[2][1] + a[2][2] * a[2][2];
+    if (!(fabs(det) > 1e-9 * sqrt(l0 * l1 * l2))) return false;  // flat: reject
+    for (int k = 0; k < 3; ++k) cen[k] = (l0 * bc[k] + l1 * ca[k] + l2 * ab[k]) / (2 * det);
+  } else {
+    double det = a[0][0] * a[1][1] - a[0][1] * a[1][0];
+    double l0 = a[0][0] * a[0][0] + a[0][1] * a[0][1], l1 = a[1][0] * a[1][0] + a[1][1] * a[1][1];
+    if (!(fabs(det) > 1e-9 * sqrt(l0 * l1))) return false;
+    cen[0] = (a[1][1] * l0 - a[0][1] * l1) / (2 * det);
+    cen[1] = (a[0][0] * l1 - a[1][0] * l0) / (2 * det);
+  }
+  rad = sqrt(cen[0] * cen[0] + cen[1] * cen[1] + cen[2] * cen[2]);
+  for (int k = 0; k < DIM; ++k) cen[k] += P0[k];
+  rad = rad * (1 + 1e-6) + 1e-7 * (fabs(cen[0]) + fabs(cen[1]) + fabs(cen[2]));
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  int64_t ncell = 1;
+  for (int k = 0; k < DIM; ++k) {
+    lo[k] = max(0, (int)floor((cen[k] - rad - g.lo[k]) * g.inv_cs) - 1);
+    hi[k] = min(g.dims[k] - 1, (int)floor((cen[k] + rad - g.lo[k]) * g.inv_cs) + 1);
+    ncell *= (hi[k] - lo[k] + 1);
+  }
+  const float r2 = (float)(rad * rad) * 1.0001f;
+  const int sx = hi[0] - lo[0] + 1, sy = hi[1] - lo[1] + 1;
+  bool inside = false;
+  for (int64_t t = lane; t < ncell && !inside; t += 32) {
+    int x = lo[0] + (int)(t % sx), y = lo[1] + (int)((t / sx) % sy),
+        z = DIM == 3 ? lo[2] + (int)(t / ((int64_t)sx * sy)) : 0;
+    float dd = 0.f;
+    int ci[3] = {x, y, z};
+    for (int k = 0; k < DIM; ++k) {
+      float b0 = g.lo[k] + ci[k] * g.cs, b1 = b0 + g.cs;
+      float cc = (float)cen[k];
+      float e = cc < b0 ? b0 - cc : (cc > b1 ? cc - b1 : 0.f);
+      dd += e * e;
+    }
+    if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
+    int c = x + g.dims[0] * (y + g.dims[1] * z);
+    for (int i = A.cell_start[c]; i < A.cell_start[c + 1] && !inside; ++i) {
+      int j = A.sorted[i];
+      if (j == ip || j == v[0] || j == v[1] || (DIM == 3 && j == v[2]) || A.dup[j]) continue;
+      float y3[3];
+      load_pt<DIM>(A.P, j, y3);
+      int s = DIM == 3 ? insph3_sos(P0, X[0], X[1], X[2], y3, &ovf, W)
+                       : incirc2_sos(P0, X[0], X[1], y3, &ovf, W);
+      inside = s < 0;
+    }
+  }
+  return !__any_sync(0xffffffffu, inside);
+}
+
+// Warp-cooperative ring search around cell cc: visits cells at Chebyshev
+// distance k = 0, 1, ... and calls f(j) for their points; after ring k,
+// every point within guard(k) of the centre x was visited.  Stops once
+// done(guard) is true or the grid is exhausted.
+template <int DIM, typename F, typename D>
+__device__ __forceinline__ void ring_search(const DTArgs &A, const GridParams &g,
+                                            const float *x, int lane, F f, D done) {
+  int cc[3] = {0, 0, 0};
+  for (int k = 0; k < DIM; ++k) cc[k] = cell_coord(g, x[k], k);
+  int kmax = 0;
+  for (int k = 0; k < DIM; ++k) kmax = max(kmax, max(cc[k], g.dims[k] - 1 - cc[k]));
+  for (int r = 0; r <= kmax; ++r) {
+    const int w = 2 * r + 1;
+    const int64_t ncell = DIM == 3 ? (int64_t)w * w * w : (int64_t)w * w;
+    for (int64_t t = lane; t < ncell; t += 32) {
+      int d0 = (int)(t % w) - r, d1 = (int)((t / w) % w) - r,
+          d2 = DIM == 3 ? (int)(t / ((int64_t)w * w)) - r : 0;
+      if (max(abs(d0), max(abs(d1), abs(d2))) != r) continue;  // ring only
+      int xx = cc[0] + d0, yy = cc[1] + d1, zz = DIM == 3 ? cc[2] + d2 : 0;
+      if (xx < 0 || yy < 0 || zz < 0 || xx >= g.dims[0] || yy >= g.dims[1] ||
+          (DIM == 3 && zz >= g.dims[2]))
+        continue;
+      int c = xx + g.dims[0] * (yy + g.dims[1] * zz);
+      for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) f(A.sorted[i]);
+    }
+    float guard = FLT_MAX;
+    for (int k = 0; k < DIM; ++k) {
+      if (cc[k] - r > 0) guard = fminf(guard, x[k] - (g.lo[k] + (cc[k] - r) * g.cs));
+      if (cc[k] + r + 1 < g.dims[k]) guard = fminf(guard, (g.lo[k] + (cc[k] + r + 1) * g.cs) - x[k]);
+    }
+    guard *= (1.f - 1e-5f);
+    if (done(guard)) return;
+  }
+}
+
+// global seed from the nearest neighbour q1 and the smallest circumcircle
+// through (p, q1): for points in general position the triangle (p, q1, q2)
+// is Delaunay and both cells on its sides are found by exhaustive queries;
+// the candidate cell is verified empty over the whole point set.
+__device__ __forceinline__ bool gseed3_nn(const DTArgs &A, const GridParams &g, int ip,
+                                          int lane, int &ovf, dmp::ExactScratch *W,
+                                          int3 &out) {
+  float px[3];
+  load_pt<3>(A.P, ip, px);
+  float bk = FLT_MAX;
+  int bj = -1, bg = 0x7fffffff;
+  ring_search<3>(A, g, px, lane,
+                 [&](int j) {
+                   if (j == ip || A.dup[j]) return;
+                   float y[3];
+                   load_pt<3>(A.P, j, y);
+                   float d = (y[0] - px[0]) * (y[0] - px[0]) + (y[1] - px[1]) * (y[1] - px[1]) +
+                             (y[2] - px[2]) * (y[2] - px[2]);
+                   if (bj < 0 || d < bk || (d == bk && j < bg)) {
+                     bk = d;
+                     bj = j;
+                     bg = j;
+                   }
+                 },
+                 [&](float guard) {
+                   float k2 = bk;
+                   int j2 = bj, g2 = bg;
+                   warp_argmin(k2, j2, g2);
+                   return j2 >= 0 && sqrtf(k2) < guard;
+                 });
+  warp_argmin(bk, bj, bg);
+  if (bj < 0) return false;
+  const int q1 = bj;
+  float a[3];
+  load_pt<3>(A.P, q1, a);
+  float A3[3] = {a[0] - px[0], a[1] - px[1], a[2] - px[2]};
+  float m[3] = {0.5f * (a[0] + px[0]), 0.5f * (a[1] + px[1]), 0.5f * (a[2] + px[2])};
+  float ck = FLT_MAX;
+  int cj = -1, cg = 0x7fffffff;
+  ring_search<3>(A, g, m, lane,
+                 [&](int j) {
+                   if (j == ip || j == q1 || A.dup[j]) return;
+                   float y[3];
+                   load_pt<3>(A.P, j, y);
+                   float B[3] = {y[0] - px[0], y[1] - px[1], y[2] - px[2]};
+                   float cx = A3[1] * B[2] - A3[2] * B[1], cy = A3[2] * B[0] - A3[0] * B[2],
+                         cz = A3[0] * B[1] - A3[1] * B[0];
+                   float cr = cx * cx + cy * cy + cz * cz;
+                   if (!(cr > 0.f)) return;
+                   float la = A3[0] * A3[0] + A3[1] * A3[1] + A3[2] * A3[2];
+                   float lb = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+                   float dx = A3[0] - B[0], dy = A3[1] - B[1], dz = A3[2] - B[2];
+                   float R2 = la * lb * (dx * dx + dy * dy + dz * dz) / (4.f * cr);
+                   if (cj < 0 || R2 < ck || (R2 == ck && j < cg)) {
+                     ck = R2;
+                     cj = j;
+                     cg = j;
+                   }
+                 },
+                 [&](float guard) {
+                   float k2 = ck;
+                   int j2 = cj, g2 = cg;
+                   warp_argmin(k2, j2, g2);
+                   // a smaller circumcircle through p and q1 lies within 2R of m
+                   return j2 >= 0 && 2.f * sqrtf(k2) * 1.0001f < guard;
+                 });
+  warp_argmin(ck, cj, cg);
+  if (cj < 0) return false;
+  const int q2 = cj;
+  for (int side = 0; side < 2; ++side) {
+    int u = side ? q2 : q1, v = side ? q1 : q2;
+    int x = gq3(A, g, ip, u, v, lane, ovf, W);
+    if (x < 0) continue;
+    int vv[3] = {u, v, x};
+    if (gempty<3>(A, g, ip, vv, lane, ovf, W)) {
+      out = make_int3(u, v, x);
+      return true;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool gseed2_nn(const DTArgs &A, const GridParams &g, int ip,
+                                          int lane, int &ovf, dmp::ExactScratch *W,
+                                          int &oa, int &ob) {
+  float px[3];
+  load_pt<2>(A.P, ip, px);
+  float bk = FLT_MAX;
+  int bj = -1, bg = 0x7fffffff;
+  ring_search<2>(A, g, px, lane,
+                 [&](int j) {
+                   if (j == ip || A.dup[j]) return;
+                   float y[3];
+                   load_pt<2>(A.P, j, y);
+                   float d = (y[0] - px[0]) * (y[0] - px[0]) + (y[1] - px[1]) * (y[1] - px[1]);
+                   if (bj < 0 || d < bk || (d == bk && j < bg)) {
+                     bk = d;
+                     bj = j;
+                     bg = j;
+                   }
+                 },
+                 [&](float guard) {
+                   float k2 = bk;
+                   int j2 = bj, g2 = bg;
+                   warp_argmin(k2, j2, g2);
+                   return j2 >= 0 && sqrtf(k2) < guard;
+                 });
+  warp_argmin(bk, bj, bg);
+  if (bj < 0) return false;
+  const int q1 = bj;
+  for (int sgn = 1; sgn >= -1; sgn -= 2) {
+    int x = gq2(A, g, ip, q1, sgn, lane, ovf, W);
+    if (x < 0) continue;
+    int a = sgn > 0 ? q1 : x, b = sgn > 0 ? x : q1;
+    int vv[3] = {a, b, -1};
+    if (gempty<2>(A, g, ip, vv, lane, ovf, W)) {
+      oa = a;
+      ob = b;
+      return true;
+    }
+  }
+  return false;
+}
+
+// Seed for the exhaustive level: local candidate pools of growing size,
+// the local seed cell kept when its circumball lies inside the pool's
+// covered radius or when it is empty over the whole point set.
+__device__ __forceinline__ bool gseed3(WarpL1<3> &Q, const DTArgs &A, const GridParams &g,
+                                       int ip, int lane, int &ovf, dmp::ExactScratch *W,
+                                       int3 &out) {
+  float px[3];
+  load_pt<3>(A.P, ip, px);
+  for (int K = 2; K <= 8; K *= 2) {
+    gather_l1<3>(Q, A, g, ip, px, lane, K);
+    if (Q.nc < 3) continue;
+    uint32_t t = seed3L(Q, A.P, ip, lane, ovf, W);
+    if (t == 0xffffffffu) continue;
+    int v[3] = {Q.id[un0(t)], Q.id[un1(t)], Q.id[un2(t)]};
+    bool ok = certified3(Q.c[un0(t)], Q.c[un1(t)], Q.c[un2(t)], Q.reff);
+    if (!ok) ok = gempty<3>(A, g, ip, v, lane, ovf, W);
+    if (ok) {
+      out = make_int3(v[0], v[1], v[2]);
+      return true;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ bool gseed2(WarpL1<2> &Q, const DTArgs &A, const GridParams &g,
+                                       int ip, int lane, int &ovf, dmp::ExactScratch *W,
+                                       int &oa, int &ob) {
+  float px[3];
+  load_pt<2>(A.P, ip, px);
+  for (int K = 3; K <= 12; K *= 2) {
+    gather_l1<2>(Q, A, g, ip, px, lane, K);
+    if (Q.nc < 2) continue;
+    uint32_t t = seed2L(Q, A.P, ip, lane, ovf, W);
+    if (t == 0xffffffffu) continue;
+    int v[3] = {Q.id[un0(t)], Q.id[un1(t)], -1};
+    bool ok = certified2(Q.c[un0(t)], Q.c[un1(t)], Q.reff);
+    if (!ok) ok = gempty<2>(A, g, ip, v, lane, ovf, W);
+    if (ok) {
+      oa = v[0];
+      ob = v[1];
+      return true;
+    }
+  }
+  return false;
+}
+
 __device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane) {
   int hit = -1;
   for (int k = lane; k < S.nopen; k += 32) {
@@ -1431,10 +1768,12 @@ __device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane
 
 __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
+  __shared__ WarpL1<3> sm1[L2_WARPS];
   dmp::ExactScratch WS;
   dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpL2 &S = sm[w];
+  auto &Q1 = sm1[w];
   const GridParams g = *A.gp;
   const int64_t nesc = A.counters[DM_CNT_ESCALATED];
   for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
@@ -1446,25 +1785,9 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
     int3 seed = make_int3(-1, -1, -1);
     if (certified) {
       seed = make_int3(sd.y, sd.z, sd.w);
-    } else if (sd.w >= 0) {
-      int f[3][2] = {{sd.y, sd.z}, {sd.z, sd.w}, {sd.w, sd.y}};
-      for (int t = 0; t < 3 && seed.x < 0; ++t) {
-        int a = f[t][0], b = f[t][1];
-        int xp = gq3(A, g, ip, a, b, lane, ovf, W);
-        int xm = gq3(A, g, ip, b, a, lane, ovf, W);
-        if (xp < 0 && xm < 0) continue;
-        bool ok = true;
-        if (xp >= 0 && xm >= 0) {
-          float pr[3], ar[3], br[3], xr[3], mr[3];
-          load_pt<3>(A.P, ip, pr);
-          load_pt<3>(A.P, a, ar);
-          load_pt<3>(A.P, b, br);
-          load_pt<3>(A.P, xp, xr);
-          load_pt<3>(A.P, xm, mr);
-          ok = insph3_sos(pr, ar, br, xr, mr, &ovf, W) > 0;
-        }
-        if (ok) seed = xp >= 0 ? make_int3(a, b, xp) : make_int3(b, a, xm);
-      }
+    } else if (!gseed3(Q1, A, g, ip, lane, ovf, W, seed) &&
+               !gseed3_nn(A, g, ip, lane, ovf, W, seed)) {
+      seed = make_int3(-1, -1, -1);
     }
     if (seed.x < 0) {
       if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
@@ -1542,10 +1865,12 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
 
 __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
+  __shared__ WarpL1<2> sm1[L2_WARPS];
   dmp::ExactScratch WS;
   dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpL2 &S = sm[w];
+  auto &Q1 = sm1[w];
   const GridParams g = *A.gp;
   const int64_t nesc = A.counters[DM_CNT_ESCALATED];
   for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
@@ -1558,34 +1883,9 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
     if (certified) {
       a = sd.y;
       b = sd.z;
-    } else {
-      // nearest-point edge candidates from the level-1 record, else exhaustive
-      int cand[2] = {sd.y, sd.z};
-      for (int t = 0; t < 2 && a < 0; ++t) {
-        int q1 = cand[t];
-        if (q1 < 0) continue;
-        int xp = gq2(A, g, ip, q1, +1, lane, ovf, W);
-        int xm = gq2(A, g, ip, q1, -1, lane, ovf, W);
-        if (xp < 0 && xm < 0) continue;
-        bool ok = true;
-        if (xp >= 0 && xm >= 0) {
-          float pr[2], qr[2], xr[2], mr[2];
-          load_pt<2>(A.P, ip, pr);
-          load_pt<2>(A.P, q1, qr);
-          load_pt<2>(A.P, xp, xr);
-          load_pt<2>(A.P, xm, mr);
-          ok = incirc2_sos(pr, qr, xr, mr, &ovf, W) > 0;
-        }
-        if (ok) {
-          if (xp >= 0) {
-            a = q1;
-            b = xp;
-          } else {
-            a = xm;
-            b = q1;
-          }
-        }
-      }
+    } else if (!gseed2(Q1, A, g, ip, lane, ovf, W, a, b) &&
+               !gseed2_nn(A, g, ip, lane, ovf, W, a, b)) {
+      a = -1;
     }
     if (a < 0) {
       if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
@@ -1670,6 +1970,9 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
 }
 
 // ---------------------------------------------------------------------------
+static int g_dbg_vertex = -1;
+static int32_t *g_dbg = nullptr;
+
 int delaunay_workspace(int dim, int64_t n, size_t *bytes) {
   Carve c(nullptr, 0);
   DTArgs a;
@@ -1699,6 +2002,8 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   a.cells = cells;
   a.cap_cells_out = cap_cells;
   a.counters = counters;
+  a.dbg_vertex = g_dbg_vertex;
+  a.dbg = g_dbg;
   DM_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int64_t) * DM_NCOUNTERS, s));
   if (n == 0) return DM_OK;
   DM_CUDA_TRY(cudaMemsetAsync(a.cell_cnt, 0, sizeof(int32_t) * a.cap_cells, s));
@@ -1840,4 +2145,24 @@ extern "C" int dmdbg_fp64(const double *a, const double *b, const double *c,
                           int32_t m, int32_t op, double *out, void *stream) {
   dm::k_debug_fp64<<<(m + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a, b, c, m, op, out);
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Debug aid: copy the escalation list and seeds of the last dm_delaunay call.
+extern "C" int dmdbg_escalations(int32_t dim, int64_t n, void *ws, size_t ws_bytes,
+                                 int32_t *esc_out, int32_t *seed_out, void *stream) {
+  using namespace dm;
+  Carve c(ws, ws_bytes);
+  DTArgs a;
+  carve_dt(c, a, dim, n);
+  cudaMemcpyAsync(esc_out, a.esc, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+  cudaMemcpyAsync(seed_out, a.esc_seed, sizeof(int4) * n, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Debug aid: make the next dm_delaunay calls dump the level-1 state of one
+// vertex into dbg (device, >= 8 + 128 + 3*128 ints); vertex -1 disables.
+extern "C" int dmdbg_watch_vertex(int32_t vertex, int32_t *dbg) {
+  dm::g_dbg_vertex = vertex;
+  dm::g_dbg = dbg;
+  return 0;
 }

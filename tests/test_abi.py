@@ -1,0 +1,114 @@
+"""C-ABI checks that need no GPU: exports, host predicates, program encoding."""
+import os
+import random
+import re
+from fractions import Fraction as Fr
+
+import numpy as np
+
+from conftest import ROOT
+from seismicmesh_gb300 import _native as N
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "dmgb.h")).read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(dm_\w+)\(", src, re.M)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    L = N.lib()
+    names = _declared()
+    assert len(names) >= 30
+    for name in names:
+        assert hasattr(L, name), name
+        assert name in N.SIGNATURES, f"{name} has no ctypes signature"
+    assert L.dm_abi_count() == len(names)
+    assert L.dm_version() >= 10000
+
+
+def test_error_reporting_on_bad_arguments():
+    L = N.lib()
+    nbytes = N.c_sz(0)
+    assert L.dm_delaunay_workspace_size(3, 1000, nbytes) == N.DM_OK and nbytes.value > 0
+    rc = L.dm_delaunay(4, None, 10, None, 0, None, None, 0, None)
+    assert rc == N.DM_ERR_ARG
+    assert b"dim" in L.dm_last_error()
+
+
+def _F(x):
+    return Fr(float(x))
+
+
+def _det(M):
+    if len(M) == 1:
+        return M[0][0]
+    return sum((-1) ** j * M[0][j] * _det([r[:j] + r[j + 1:] for r in M[1:]]) for j in range(len(M)) if M[0][j] != 0)
+
+
+def _sgn(x):
+    return (x > 0) - (x < 0)
+
+
+def _insph_sos_ref(P):
+    """sign of the lifted 5x5 determinant with lift perturbation eps^rank,
+    rank by lexicographic order (largest first), in exact rationals"""
+    a = P[0]
+    rows = []
+    for q in P[1:]:
+        v = [_F(q[i]) - _F(a[i]) for i in range(3)]
+        rows.append(v + [sum(x * x for x in v)])
+    base = _det(rows)
+    if base != 0:
+        return _sgn(base)
+    order = sorted(range(5), key=lambda i: tuple(float(x) for x in P[i]), reverse=True)
+    eps = Fr(1, 10**40)
+    delta = [0] * 5
+    for r, i in enumerate(order):
+        delta[i] = eps ** (r + 1)
+    rows = []
+    for k, q in enumerate(P[1:], 1):
+        v = [_F(q[i]) - _F(a[i]) for i in range(3)]
+        rows.append(v + [sum(x * x for x in v) + delta[k] - delta[0]])
+    return _sgn(_det(rows))
+
+
+def test_host_predicates_exact_against_rationals():
+    L = N.lib()
+    rng = random.Random(7)
+    fp = N.fptr
+    degenerate = 0
+    for t in range(1500):
+        if t % 3 == 0:
+            P = [np.float32([rng.uniform(-1, 1) for _ in range(3)]) for _ in range(5)]
+        elif t % 3 == 1:
+            P = []
+            for _ in range(5):
+                v = np.array([rng.gauss(0, 1) for _ in range(3)])
+                P.append(np.float32(0.3 + 0.02 * v / np.linalg.norm(v)))
+        else:
+            P = [np.float32([0.5 * rng.randint(-2, 2), 0.5 * rng.randint(-2, 2) + 0.25 * rng.randint(0, 1),
+                             0.5 * rng.randint(-2, 2)]) for _ in range(5)]
+        if len({tuple(p) for p in P}) < 5:
+            continue
+        o = _sgn(_det([[_F(q[i]) - _F(P[0][i]) for i in range(3)] for q in P[1:4]]))
+        assert L.dm_orient3(*[fp(p) for p in P[:4]]) == o
+        for k in (0, 1):  # exact and FP64-filtered stages alone
+            assert L.dmdbg_host_pred(k, *[fp(p) for p in P[:4]], fp(P[4])) == o
+        if o == 0:
+            continue
+        s = _insph_sos_ref(P)
+        degenerate += 0
+        assert L.dm_insphere_sos(*[fp(p) for p in P]) == s
+    assert degenerate == 0
+
+
+def test_sdf_program_encoding():
+    import seismicmesh_gb300 as sm
+
+    d = sm.Difference([sm.Ball((0, 0, 0.5), 0.85), sm.Cube((-0.5, 0.5, -0.5, 0.5, -0.5, 0.5))], smoothness=0.2)
+    prog = d.program()
+    assert [op[0] for op in prog.ops] == [2, 4, 22]
+    assert prog.ops[-1][2] == 2 and prog.params[prog.ops[-1][1]] == np.float32(0.2)
+    r = sm.Rectangle((0.0, 1.0, 0.0, 1.0), rotate=[0.3, 0, 0], translate=[0.1, 0.2])
+    op = r.program().ops[0]
+    assert op[0] == 3 and op[3] == (1 | 2)  # translate + 2D rotation

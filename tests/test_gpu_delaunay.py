@@ -1,0 +1,92 @@
+"""GPU Delaunay (dm_delaunay) against the oracle.
+
+Generic inputs: identical to Qhull after canonical ordering.  Exactly
+degenerate lattices: a valid triangulation of the convex hull whose cells
+are positively oriented and whose circumspheres are empty under the
+symbolic perturbation (checked with the host exact predicates)."""
+import numpy as np
+import pytest
+import torch
+from scipy.spatial import ConvexHull, cKDTree
+
+from oracle import delaunay_check as dc
+from seismicmesh_gb300 import _native as N
+from seismicmesh_gb300.generation.mesh_generator import _Engine
+from seismicmesh_gb300.generation.utils import create_staggered_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def triangulate(p):
+    eng = _Engine(p.shape[1], p, 0)
+    nc = eng.triangulate()
+    return eng.cells[:nc].cpu().numpy(), eng.counters_host()
+
+
+@pytest.mark.parametrize("dim,n", [(2, 10), (2, 300), (2, 20000), (3, 12), (3, 300), (3, 20000)])
+def test_random_points_match_qhull(cuda, dim, n):
+    rng = np.random.default_rng(dim * 1000 + n)
+    p = rng.random((n, dim)).astype(np.float32).astype(np.float64)
+    cells, c = triangulate(p)
+    assert c[N.CNT_FLAGS] == 0
+    dc.assert_same_triangulation(p, cells)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_clustered_points_match_qhull(cuda, dim):
+    """strongly non-uniform density (exercises the exhaustive level)"""
+    rng = np.random.default_rng(11)
+    a = rng.normal(0, 0.01, (3000, dim))
+    b = rng.uniform(-1, 1, (2000, dim))
+    p = np.vstack([a, b]).astype(np.float32).astype(np.float64)
+    cells, c = triangulate(p)
+    assert c[N.CNT_FLAGS] == 0
+    dc.assert_same_triangulation(p, cells)
+
+
+def _check_valid(p, cells, dim, max_checks=4000):
+    L = N.lib()
+    p32 = p.astype(np.float32)
+    fp = lambda a: np.ascontiguousarray(a, np.float32).ctypes.data_as(N._FP)  # noqa: E731
+    for c in cells:
+        s = L.dm_orient3(*[fp(p32[i]) for i in c]) if dim == 3 else L.dm_orient2(*[fp(p32[i]) for i in c])
+        assert s > 0
+    d = p[cells[:, 1:]] - p[cells[:, :1]]
+    vol = np.abs(np.linalg.det(d)).sum() / (6 if dim == 3 else 2)
+    assert abs(vol - ConvexHull(p).volume) < 1e-9 * max(1.0, vol)
+    tree = cKDTree(p)
+    checked = 0
+    for c in cells[:max_checks]:
+        P = p[c]
+        A = 2 * (P[1:] - P[0])
+        b = (P[1:] ** 2).sum(1) - (P[0] ** 2).sum()
+        cen = np.linalg.solve(A, b)
+        r = np.linalg.norm(P[0] - cen)
+        for j in tree.query_ball_point(cen, r * 1.001 + 1e-9):
+            if j in c:
+                continue
+            checked += 1
+            if dim == 3:
+                s = L.dm_insphere_sos(*[fp(p32[i]) for i in c], fp(p32[j]))
+            else:
+                s = L.dm_incircle_sos(*[fp(p32[i]) for i in c], fp(p32[j]))
+            assert s > 0, (c, j)
+    return checked
+
+
+@pytest.mark.parametrize("dim,h", [(2, 0.25), (2, 0.05), (3, 0.5), (3, 0.25)])
+def test_degenerate_lattice_is_valid_perturbed_delaunay(cuda, dim, h):
+    p = create_staggered_grid(h, dim, np.array([[-1.0, 1.0]] * dim)).astype(np.float32).astype(np.float64)
+    cells, c = triangulate(p)
+    assert c[N.CNT_FLAGS] == 0
+    _check_valid(p, cells, dim)
+
+
+def test_duplicate_points_are_merged_like_cgal(cuda):
+    rng = np.random.default_rng(3)
+    p = rng.random((500, 3)).astype(np.float32).astype(np.float64)
+    q = np.vstack([p, p[:20]])
+    eng = _Engine(3, q, 0)
+    nc = eng.triangulate()
+    assert eng.n == 500
+    dc.assert_same_triangulation(eng.P[:, :3].double().cpu().numpy(), eng.cells[:nc].cpu().numpy())
