@@ -1,0 +1,379 @@
+"""Benchmark: DistMesh point-iterations/s and time-to-mesh on one GB300.
+
+Workload: 3D unit ball (Ball((0,0,0), 1)), constant edge length h = 0.02,
+526,727 initial vertices, max_iter 50, seed 0, then sliver_removal with a
+10 degree minimum dihedral angle.
+
+  step    one DistMesh iteration on the device-resident point set:
+          dm_delaunay -> dm_filter_cells -> dm_adjacency -> dm_bar_sums ->
+          dm_update_points.  The first W (warm-up) iterations start from the
+          initial lattice; the K timed iterations follow.  Each step is timed
+          with CUDA events on the launching stream; a 256 MB buffer is written
+          between steps so L2 (129 MB) holds none of the step's inputs.
+  value   point-iterations/s = n_points * K / sum(step times).
+  e2e     the same metric through the public API from host data:
+          generate_mesh(Ball, 0.02) + sliver_removal, host numpy in, host
+          numpy out; e2e value = n_points * (max_iter - 1) / wall time of
+          generate_mesh; time_to_mesh_s includes sliver_removal.
+
+--impl reference times the reference's CPU loop (the oracle's float64 numpy
+restatement with Qhull connectivity; CGAL and MPI are not available) on a
+bounded sample of the workload, the same ball at h = 0.04 (66,394 points).
+With torchrun (N > 1) every rank meshes its own replica; value is the sum
+over ranks (timed with a barrier and the max over ranks).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+H = 0.02
+SAMPLE_H = 0.04
+METRIC = "point-iterations/s (3D unit ball, h=0.02, DistMesh iterations)"
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def reduce_max(x, world, backend):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if backend == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region"""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        cmd = [
+            "nvidia-smi", f"--id={self.index}",
+            "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+            "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+            "clocks_event_reasons.sw_power_cap",
+            "--format=csv,noheader,nounits", "-lms", "200",
+        ]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 3 + k and r[3 + k].lower() == "active":
+                    reasons.add(nm)
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": mx,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(steps, warmup):
+    """the oracle's restatement of the reference loop on the h = 0.04 ball"""
+    from oracle import distmesh_np as O
+    from oracle import sdf_np as S
+
+    fd = S.ball(0.0, 0.0, 0.0, 1.0)
+    fh = lambda x: np.full(len(x), SAMPLE_H)  # noqa: E731
+    bbox = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    p = O.initial_points(fd, fh, SAMPLE_H, bbox, 0.1 * SAMPLE_H, 3)
+    for _ in range(warmup):
+        p, _, _ = O.one_iteration(p, fd, fh, SAMPLE_H)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        p, _, _ = O.one_iteration(p, fd, fh, SAMPLE_H)
+    dt = time.perf_counter() - t0
+    return len(p), dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    n, dt = cpu_sample(args.steps, args.warmup)
+    value = n * args.steps / dt
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "point-iterations/s",
+        "impl": "reference",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dt / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (initial lattice of the unit ball, seeded decimation)",
+        "config": {"workload": "3D unit ball h=0.04 sample of the h=0.02 ball (66,394 points), "
+                               "one DistMesh iteration per step", "n_points": n},
+        "cpu_baseline": {
+            "value": value, "unit": "point-iterations/s", "cores": 1, "kind": "port",
+            "sample": f"{args.steps} DistMesh iterations of the h=0.04 unit ball ({n} points), "
+                      "float64 numpy restatement of the reference loop, Qhull connectivity "
+                      "(CGAL not installable), serial",
+        },
+        "e2e": {"value": value, "unit": "point-iterations/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import ctypes
+
+    import torch
+
+    from seismicmesh_gb300 import _build
+
+    _build.build_library()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import seismicmesh_gb300 as sm
+    from seismicmesh_gb300 import _device as D
+    from seismicmesh_gb300 import _native as N
+    from seismicmesh_gb300.generation import mesh_generator as MG
+
+    L = N.lib()
+    L.dmprof_read.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_int32)]
+    L.dmprof_launches.restype = ctypes.c_int64
+
+    ball = sm.Ball([0.0, 0.0, 0.0], 1.0)
+    fd = MG._Domain(ball)
+    sizing = MG._Sizing(H, 3)
+    opts = {"points": None, "r0m_is_h0": False, "seed": 0}
+    p0 = MG._initialize_points(3, 0.1 * H, np.array([[-1.0, 1.0]] * 3), sizing, fd, H, opts, np.empty((0, 3)))
+    n = len(p0)
+    L0mult = 1 + 0.4 / 2 ** 2
+    deps = float(np.sqrt(np.finfo(float).eps) * H)
+    eng = MG._Engine(3, p0, 0)
+    levels = [fd]
+    lv = (N.SdfProgram * 1)()
+    lv[0] = fd.program().struct
+    prog = fd.program().struct
+    stream = D.stream_ptr()
+
+    def iteration_async():
+        N.call("dm_delaunay", 3, D.ptr(eng.P), eng.n, D.ptr(eng.cells), eng.cap_cells,
+               D.ptr(eng.counters), D.ptr(eng.ws_dt), eng.ws_dt.numel(), stream)
+        N.call("dm_filter_cells", 3, D.ptr(eng.P), D.ptr(eng.cells), eng.cap_cells, prog,
+               0.1 * H, D.ptr(eng.kept), D.ptr(eng.counters), None, 0, stream)
+        N.call("dm_adjacency", 3, eng.n, D.ptr(eng.kept), eng.cap_cells, N.CNT_KEPT,
+               D.ptr(eng.adj), eng.adj_cap, D.ptr(eng.deg), D.ptr(eng.counters), stream)
+        N.call("dm_bar_sums", 3, D.ptr(eng.P), eng.n, D.ptr(eng.adj), eng.adj_cap,
+               D.ptr(eng.deg), sizing.struct, D.ptr(eng.partials), stream)
+        N.call("dm_update_points", 3, D.ptr(eng.P), D.ptr(eng.P2), eng.n, D.ptr(eng.adj),
+               eng.adj_cap, D.ptr(eng.deg), sizing.struct, D.ptr(eng.partials), L0mult, 0.30,
+               0, lv, 1, H, deps, D.ptr(eng.maxf), stream)
+        eng.P, eng.P2 = eng.P2, eng.P
+
+    # warm-up: the checked path (duplicates / capacity handled)
+    for _ in range(args.warmup):
+        eng.triangulate()
+        eng.filter(fd, 0.1 * H)
+        eng.build_adjacency()
+        eng.step(sizing, levels, L0mult, 0.30, H, deps)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = L.dmprof_launches()
+    L.dmprof_enable(1)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record()
+            iteration_async()
+            ev[k][1].record()
+        torch.cuda.synchronize()
+    barrier(world)
+    L.dmprof_enable(0)
+    launches = L.dmprof_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    c = eng.counters_host()
+    flags = int(c[N.CNT_FLAGS])
+    if flags:
+        raise RuntimeError(f"device flags {flags:#x} during the timed iterations")
+    ms1, ms2, calls = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+    L.dmprof_read(ms1, ms2, calls)
+    n_cells = int(c[N.CNT_CELLS])
+    max_ms = reduce_max(total_ms, world, "nccl")
+    value = world * n * args.steps / (max_ms / 1000.0)
+
+    # roofline of the dominant kernel (level-1 star kernel of dm_delaunay):
+    # algorithmic bytes per launch = points read (16 B each) + cells written
+    # (16 B each) + candidate grid reads (4 B per point for the sorted ids and
+    # 8 B per cell range), i.e. 16 n + 16 T + 4 n + 8 n_cells_grid ~ 16 T + 28 n
+    l1_ms = ms1.value / max(calls.value, 1)
+    l2_ms = ms2.value / max(calls.value, 1)
+    alg_bytes = 16 * n_cells + 28 * n
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (l1_ms / 1000.0) / 1e9
+
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts, cells = sm.generate_mesh(ball, H, verbose=0)
+        t1 = time.perf_counter()
+        pts2, cells2 = sm.sliver_removal(pts, ball, H, verbose=0)
+        t2 = time.perf_counter()
+        gen_s, sliver_s = t1 - t0, t2 - t1
+        e2e_val = n * 49 / gen_s
+        e2e = {
+            "value": reduce_max(e2e_val, world, "nccl") if world == 1 else e2e_val * world,
+            "unit": "point-iterations/s",
+            "h2d_bytes_per_step": int(n * 16 / 49),
+            "d2h_bytes_per_step": int((pts.nbytes + cells.nbytes) / 49),
+            "time_to_mesh_s": gen_s + sliver_s,
+            "generate_mesh_s": gen_s,
+            "sliver_removal_s": sliver_s,
+            "final_points": int(len(pts2)),
+            "final_cells": int(len(cells2)),
+        }
+        from oracle import distmesh_np as O
+
+        dh = np.degrees(O.dihedral_angles(pts2, cells2)).reshape(-1, 6).min(1)
+        e2e["min_dihedral_deg"] = float(dh.min())
+        e2e["mean_min_dihedral_deg"] = float(dh.mean())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ncpu, dt = cpu_sample(2, 0)
+        cpu = {
+            "value": ncpu * 2 / dt, "unit": "point-iterations/s", "cores": 1, "kind": "port",
+            "sample": f"2 DistMesh iterations of the h=0.04 unit ball ({ncpu} points), float64 numpy "
+                      "restatement of the reference loop with Qhull connectivity, serial",
+        }
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "point-iterations/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": max_ms / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32 (positions, forces); exact f64 expansions in the predicates",
+            "data": "synthetic (initial lattice of the unit ball, seeded decimation)",
+            "config": {
+                "workload": "3D unit ball, h=0.02, DistMesh iterations after 'warmup' iterations from the initial lattice",
+                "n_points": n,
+                "n_cells": n_cells,
+                "l2": "256 MB buffer written between timed steps",
+                "parallelism": f"replicas x{world}",
+            },
+            "roofline": {
+                "bound": "hbm",
+                "kernel": "k_star3_l1 (vertex-star Delaunay, level 1)",
+                "achieved": achieved,
+                "peak": peak,
+                "peak_kind": peak_kind,
+                "unit": "GB/s",
+                "frac": achieved / peak,
+                "traffic": None,
+                "alg_bytes_per_launch": alg_bytes,
+                "avg_launch_ms": l1_ms,
+                "level2_ms": l2_ms,
+            },
+            "phases_ms": {"step_ms_min": min(step_ms), "step_ms_max": max(step_ms)},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

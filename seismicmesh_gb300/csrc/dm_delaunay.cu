@@ -1973,6 +1973,22 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
 static int g_dbg_vertex = -1;
 static int32_t *g_dbg = nullptr;
 
+// Optional timing of the star kernels (events on the caller's stream).
+constexpr int kProfMax = 256;
+static bool g_prof_on = false;
+static int g_prof_n = 0;
+static cudaEvent_t g_prof_ev[kProfMax][3];
+static int64_t g_launches = 0;
+
+void note_launches(int k) { g_launches += k; }
+
+static void prof_mark(int slot, cudaStream_t s) {
+  if (!g_prof_on || g_prof_n >= kProfMax) return;
+  cudaEvent_t &e = g_prof_ev[g_prof_n][slot];
+  if (!e) cudaEventCreate(&e);
+  cudaEventRecord(e, s);
+}
+
 int delaunay_workspace(int dim, int64_t n, size_t *bytes) {
   Carve c(nullptr, 0);
   DTArgs a;
@@ -2037,17 +2053,22 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   // kernels still run on the single-cell grid and stay bounded)
   int64_t nwb = (n + L1_WARPS - 1) / L1_WARPS;
   int g1 = (int)std::min<int64_t>(nwb, (int64_t)kSMs * 16);
+  prof_mark(0, s);
   if (dim == 3)
     k_star3_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
   else
     k_star2_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
   DM_LAUNCH_CHECK();
+  prof_mark(1, s);
   int g2 = kSMs * 8;
   if (dim == 3)
     k_star3_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
   else
     k_star2_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
   DM_LAUNCH_CHECK();
+  prof_mark(2, s);
+  if (g_prof_on && g_prof_n < kProfMax) ++g_prof_n;
+  note_launches(12);
   return DM_OK;
 }
 
@@ -2166,3 +2187,29 @@ extern "C" int dmdbg_watch_vertex(int32_t vertex, int32_t *dbg) {
   dm::g_dbg = dbg;
   return 0;
 }
+
+// Timing of the star kernels of the dm_delaunay calls made while enabled:
+// dmprof_enable(1) resets and starts; dmprof_read synchronises the events and
+// returns the summed milliseconds of level 1 and level 2 and the call count.
+extern "C" int dmprof_enable(int32_t on) {
+  dm::g_prof_on = on != 0;
+  dm::g_prof_n = 0;
+  return 0;
+}
+extern "C" int dmprof_read(double *ms_l1, double *ms_l2, int32_t *calls) {
+  double a = 0, b = 0;
+  for (int i = 0; i < dm::g_prof_n; ++i) {
+    float t1 = 0, t2 = 0;
+    cudaEventSynchronize(dm::g_prof_ev[i][2]);
+    cudaEventElapsedTime(&t1, dm::g_prof_ev[i][0], dm::g_prof_ev[i][1]);
+    cudaEventElapsedTime(&t2, dm::g_prof_ev[i][1], dm::g_prof_ev[i][2]);
+    a += t1;
+    b += t2;
+  }
+  *ms_l1 = a;
+  *ms_l2 = b;
+  *calls = dm::g_prof_n;
+  return 0;
+}
+// number of kernels libdmgb.so has launched in this process
+extern "C" int64_t dmprof_launches(void) { return dm::g_launches; }

@@ -7,6 +7,8 @@
 
 namespace dm {
 
+void note_launches(int k);
+
 struct SdfDev {
   const int32_t *ops;
   const float *params;
@@ -637,6 +639,7 @@ int filter_cells(int dim, const float *P, const int32_t *cells, int64_t cap,
   else
     k_filter_cells<2><<<nb, 256, 0, s>>>(P, cells, cap, to_sdf(sdf), geps, out, counters);
   DM_LAUNCH_CHECK();
+  note_launches(1);
   return DM_OK;
 }
 
@@ -670,6 +673,7 @@ int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
   k_adj_sort<<<nw, 32 * ADJ_WARPS, 0, s>>>(n, adj, adj_cap, deg, counters);
   k_half_edges<<<1, 1, 0, s>>>(counters);
   DM_LAUNCH_CHECK();
+  note_launches(3);
   return DM_OK;
 }
 
@@ -693,6 +697,7 @@ int bar_sums(int dim, const float *P, int64_t n, const int32_t *adj,
     k_bar_sums<2><<<nblk, 256, 0, s>>>(P, n, adj, adj_cap, deg, d, partials);
   k_bar_scale<<<1, 1024, 0, s>>>(partials, nblk, dim);
   DM_LAUNCH_CHECK();
+  note_launches(2);
   return DM_OK;
 }
 
@@ -720,6 +725,7 @@ int update_points(int dim, const float *P, float *Pout, int64_t n,
                                      nblk, L0mult, dt, nfix, L, hmin, deps, maxf);
   k_max_reduce<<<1, 1024, 0, s>>>(maxf, nblk);
   DM_LAUNCH_CHECK();
+  note_launches(2);
   return DM_OK;
 }
 
