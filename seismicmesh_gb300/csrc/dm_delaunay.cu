@@ -2193,7 +2193,7 @@ extern "C" int dmdbg_watch_vertex(int32_t vertex, int32_t *dbg) {
 // returns the summed milliseconds of level 1 and level 2 and the call count.
 extern "C" int dmprof_enable(int32_t on) {
   dm::g_prof_on = on != 0;
-  dm::g_prof_n = 0;
+  if (on) dm::g_prof_n = 0;
   return 0;
 }
 extern "C" int dmprof_read(double *ms_l1, double *ms_l2, int32_t *calls) {
@@ -2213,3 +2213,11 @@ extern "C" int dmprof_read(double *ms_l1, double *ms_l2, int32_t *calls) {
 }
 // number of kernels libdmgb.so has launched in this process
 extern "C" int64_t dmprof_launches(void) { return dm::g_launches; }
+
+// Debug aid: read and reset the slow-path counters of the Delaunay kernels.
+extern "C" int dmprof_slow_counters(unsigned long long *out8) {
+  cudaMemcpyFromSymbol(out8, dmp::g_slow, sizeof(unsigned long long) * 8);
+  unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaMemcpyToSymbol(dmp::g_slow, z, sizeof(z));
+  return 0;
+}

@@ -49,6 +49,16 @@
 
 namespace dmp {
 
+// Slow-path event counters (device side, per translation unit), compiled in
+// only with -DDMP_SLOW_COUNTERS: [0] orient fp64 stage, [1] orient exact,
+// [2] insphere fp64 stage, [3] insphere exact, [4] symbolic perturbation.
+static __device__ unsigned long long g_slow[8];
+#if defined(__CUDA_ARCH__) && defined(DMP_SLOW_COUNTERS)
+#define DMP_COUNT(i) atomicAdd(&g_slow[i], 1ull)
+#else
+#define DMP_COUNT(i) ((void)0)
+#endif
+
 // Every operation of the error-free transformations must round on its own:
 // a multiply fused into a following add (FMA contraction, nvcc's default)
 // breaks Two-Sum.  Device code uses the explicitly rounded intrinsics, which
@@ -247,6 +257,7 @@ struct ExactScratch {
 // (Laplace expansion of det[[x y z 1]] along the ones column).
 DM_HD_NI int orient3_exact(const float *a, const float *b, const float *c,
                            const float *d, ExactScratch *W) {
+  DMP_COUNT(1);
   double(*m)[2] = W->m;  // pairs ab ac ad bc bd cd
   int nab = minor2(a, b, m[0]), nac = minor2(a, c, m[1]), nad = minor2(a, d, m[2]);
   int nbc = minor2(b, c, m[3]), nbd = minor2(b, d, m[4]), ncd = minor2(c, d, m[5]);
@@ -316,6 +327,7 @@ DM_HD int acc_add_product(int nacc, double *acc, int ncoef, const double *coef,
 DM_HD_NI int insph3_exact(const float *a, const float *b, const float *c,
                           const float *d, const float *e, int *overflow,
                           ExactScratch *W) {
+  DMP_COUNT(3);
   for (int i = 0; i < 5; ++i)
     for (int j = i + 1; j < 5; ++j) {
       int t = pair_index(i, j, 5);
@@ -488,6 +500,7 @@ DM_HD int exact_diff(const float *b, const float *a, int dim, double *out) {
 // Full predicates on raw coordinates (FP64 filter then exact).
 DM_HD int orient3_slow(const float *a, const float *b, const float *c,
                           const float *d, ExactScratch *W) {
+  DMP_COUNT(0);
   double X[3], Y[3], Z[3];
   if (exact_diff(b, a, 3, X) && exact_diff(c, a, 3, Y) && exact_diff(d, a, 3, Z)) {
     int s = orient3_rel_filter<double>(X[0], X[1], X[2], Y[0], Y[1], Y[2], Z[0],
@@ -536,6 +549,7 @@ DM_HD int orient2(const float *a, const float *b, const float *c,
 DM_HD int insph3_slow(const float *a, const float *b, const float *c,
                          const float *d, const float *e, int *overflow,
                          ExactScratch *W) {
+  DMP_COUNT(2);
   double X[3], Y[3], Z[3], Q[3];
   if (exact_diff(b, a, 3, X) && exact_diff(c, a, 3, Y) && exact_diff(d, a, 3, Z) &&
       exact_diff(e, a, 3, Q)) {
@@ -556,6 +570,7 @@ DM_HD int insph3_slow(const float *a, const float *b, const float *c,
 // perturbation) down; the first non-zero coefficient decides.
 DM_HD int insph3_sos_tail(const float *a, const float *b, const float *c,
                           const float *d, const float *e, ExactScratch *W) {
+  DMP_COUNT(4);
   int done = 0;  // bit mask of visited points
   for (int step = 0; step < 5; ++step) {
     int best = -1;
