@@ -146,6 +146,28 @@ int dm_unique_edges_workspace_size(int64_t n, int64_t m, size_t *bytes);
 int dm_unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
                     int64_t *n_out_host, void *workspace,
                     size_t workspace_bytes, void *stream);
+/* dm_unique_edges without a workspace.  No counterpart in the reference: its
+ * unique_edges (geometry/cpp/fast_geometry.cpp:30-77) works on host vectors.
+ * Same inputs, outputs and results as dm_unique_edges, but every
+ * intermediate array lives in one static device array of the library
+ * (about 8.4 MB per device), so the call allocates nothing: no cudaMalloc,
+ * no cudaFree, no allocating library routine.  It serves callers that have
+ * device buffers but cannot allocate a workspace: a thin FFI binding with no
+ * device allocator of its own, or a process whose device memory is held by a
+ * caching allocator, where an extra cudaMalloc can fail while the pool still
+ * has room and a cudaFree synchronises the whole device.
+ * Limits: n <= 131072 vertices and m <= 524288 edges; larger sizes return
+ * DM_ERR_CAPACITY with a message naming the limits.
+ * The first call on each device looks up the scratch address with
+ * cudaGetSymbolAddress (with that device current; a failure returns
+ * DM_ERR_CUDA), which may load the library's device code: make that first
+ * call (m = 0 is enough) before any stream capture begins.
+ * Nothing has to be zero beforehand: each call clears the counters it uses.
+ * One scratch exists per device, so calls that overlap in time on the same
+ * device (two streams or two host threads) race on it: serialise them.
+ * Synchronises `stream` to read the output count, like dm_unique_edges. */
+int dm_unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
+                            int32_t *out, int64_t *n_out_host, void *stream);
 
 /* ---- bar forces and point update ---------------------------------------
  * Replaces _compute_forces + dense scatter + position update + Newton

@@ -81,6 +81,7 @@ SIGNATURES = {
     "dm_adjacency": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_int, c_p, c_p, c_p]),
     "dm_unique_edges_workspace_size": (c_int, [c_i64, c_i64, ctypes.POINTER(c_sz)]),
     "dm_unique_edges": (c_int, [c_p, c_i64, c_i64, c_p, ctypes.POINTER(c_i64), c_p, c_sz, c_p]),
+    "dm_unique_edges_noalloc": (c_int, [c_p, c_i64, c_i64, c_p, ctypes.POINTER(c_i64), c_p]),
     "dm_bar_blocks": (c_int, [c_i64, ctypes.POINTER(c_int)]),
     "dm_bar_sums": (c_int, [c_int, c_p, c_i64, c_p, c_int, c_p, ctypes.POINTER(Sizing), c_p, c_p]),
     "dm_update_points": (

@@ -50,6 +50,8 @@ int limgrad(const int32_t *dims, double elen, double dfdx, int imax, double *f,
 int unique_edges_workspace(int64_t n, int64_t m, size_t *bytes);
 int unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
                  int64_t *n_out, void *ws, size_t ws_bytes, cudaStream_t s);
+int unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
+                         int32_t *out, int64_t *n_out, cudaStream_t s);
 size_t boundary_workspace(int dim, int64_t n, int64_t cap_cells);
 int boundary(int dim, int64_t n, const int32_t *cells, int64_t cap,
              int count_index, int32_t *vflag, int32_t *faces_out,
@@ -86,7 +88,7 @@ extern "C" {
 
 int dm_version(void) { return 10000; }
 const char *dm_last_error(void) { return dm::last_error(); }
-int dm_abi_count(void) { return 37; }
+int dm_abi_count(void) { return 38; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
   dmp::ExactScratch W;
@@ -159,6 +161,10 @@ int dm_unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
                     size_t workspace_bytes, void *stream) {
   return dm::unique_edges(edges, m, n, out, n_out_host, workspace,
                           workspace_bytes, S(stream));
+}
+int dm_unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
+                            int32_t *out, int64_t *n_out_host, void *stream) {
+  return dm::unique_edges_noalloc(edges, m, n, out, n_out_host, S(stream));
 }
 
 int dm_bar_blocks(int64_t n, int32_t *nblk) {

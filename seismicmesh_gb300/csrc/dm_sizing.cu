@@ -1,4 +1,6 @@
 // Gradient limiting of mesh-size grids and the drop-in unique_edges.
+#include <mutex>
+
 #include "dm_common.cuh"
 
 namespace dm {
@@ -168,6 +170,92 @@ int unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
   int nb = grid_for(m, 256);
   k_ue_count<<<nb, 256, 0, s>>>(edges, m, cnt, key, slot);
   int rc = exclusive_scan_i32(cnt, start, n, tmp, s);
+  if (rc) return rc;
+  k_ue_scatter<<<nb, 256, 0, s>>>(edges, m, start, key, slot, val);
+  k_ue_sort<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ucnt);
+  rc = exclusive_scan_i32(ucnt, ustart, n, tmp, s);
+  if (rc) return rc;
+  k_ue_write<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ustart, out);
+  DM_LAUNCH_CHECK();
+  int32_t total = 0;
+  DM_CUDA_TRY(cudaMemcpyAsync(&total, ustart + n, sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaStreamSynchronize(s));
+  *n_out = total;
+  return DM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// unique_edges on library-owned scratch: the same kernels as unique_edges,
+// with every intermediate array carved from one static device array instead
+// of a caller workspace.  Nothing is allocated.  Limits: n <= 131072
+// vertices, m <= 524288 edges.  The bucket counters are cleared at the start
+// of every call, so nothing has to be zero beforehand.  One scratch exists
+// per device: calls that overlap in time on the same device race on it.
+constexpr int64_t kUeStaticMaxN = int64_t(1) << 17;
+constexpr int64_t kUeStaticMaxM = int64_t(1) << 19;
+constexpr size_t kUeStaticBytes =
+    4 * (4 * (size_t)kUeStaticMaxN + 3 * (size_t)kUeStaticMaxM) + (64 << 10);
+constexpr int kUeMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_ue_scratch[kUeStaticBytes];
+
+static std::mutex g_ue_mu;
+static void *g_ue_addr[kUeMaxDevices];  // by device ordinal, set on first use
+
+// Address of g_ue_scratch on the current device, looked up once per device
+// with that device current.
+static int ue_static_scratch(void **out) {
+  int dev = -1;
+  DM_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kUeMaxDevices) {
+    set_error("unique_edges_noalloc: device ordinal %d outside [0, %d)", dev,
+              kUeMaxDevices);
+    return DM_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_ue_mu);
+  if (!g_ue_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_ue_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("unique_edges_noalloc: cudaGetSymbolAddress on device %d "
+                "failed: %s", dev, cudaGetErrorString(e));
+      return DM_ERR_CUDA;
+    }
+    g_ue_addr[dev] = p;
+  }
+  *out = g_ue_addr[dev];
+  return DM_OK;
+}
+
+int unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
+                         int32_t *out, int64_t *n_out, cudaStream_t s) {
+  DM_ARG_CHECK(n >= 0 && m >= 0, "sizes");
+  DM_ARG_CHECK(n_out != nullptr, "n_out");
+  if (n > kUeStaticMaxN || m > kUeStaticMaxM) {
+    set_error("unique_edges_noalloc: n = %lld vertices, m = %lld edges "
+              "exceed the static scratch limits n <= %lld, m <= %lld; use "
+              "dm_unique_edges with a workspace", (long long)n, (long long)m,
+              (long long)kUeStaticMaxN, (long long)kUeStaticMaxM);
+    return DM_ERR_CAPACITY;
+  }
+  void *base = nullptr;
+  int rc = ue_static_scratch(&base);
+  if (rc) return rc;
+  Carve c(base, kUeStaticBytes);
+  int32_t *cnt, *start, *key, *slot, *val, *ucnt, *ustart, *tmp;
+  carve_ue(c, n, m, &cnt, &start, &key, &slot, &val, &ucnt, &ustart, &tmp);
+  if (!c.ok()) {
+    set_error("unique_edges_noalloc: static scratch %zu < required %zu",
+              kUeStaticBytes, c.used);
+    return DM_ERR_WORKSPACE;
+  }
+  *n_out = 0;
+  if (m == 0 || n == 0) return DM_OK;
+  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
+  int nb = grid_for(m, 256);
+  k_ue_count<<<nb, 256, 0, s>>>(edges, m, cnt, key, slot);
+  rc = exclusive_scan_i32(cnt, start, n, tmp, s);
   if (rc) return rc;
   k_ue_scatter<<<nb, 256, 0, s>>>(edges, m, start, key, slot, val);
   k_ue_sort<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ucnt);
