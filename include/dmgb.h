@@ -182,10 +182,11 @@ int dm_unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
  *                    zero level set of every program in `levels`
  *                    (level 0: points with d > 0; level k > 0: points with
  *                    0 < d < hmin / 1.5).  Writes points_out, per-block
- *                    maxima of |F| into maxf[0..nblk) and their maximum
- *                    into maxf[nblk].
- * dm_bar_blocks gives nblk for n points; partials holds 2*nblk + 3 doubles
- * (partials[2*nblk] = the L0 scale, then sum L^d and sum h^d). */
+ *                    maxima of |F| into the leading entries of maxf and
+ *                    their maximum into maxf[nblk].
+ * dm_bar_blocks gives nblk for n points (the same for 2D and 3D); partials
+ * is a workspace of 2*nblk + 3 doubles written by dm_bar_sums and read by
+ * dm_update_points. */
 int dm_bar_blocks(int64_t n, int32_t *nblk);
 int dm_bar_sums(int32_t dim, const float *points, int64_t n,
                 const int32_t *adj, int32_t adj_cap, const int32_t *deg,

@@ -52,8 +52,14 @@ def _needs_rebuild(obj, deps):
 
 def build_library(verbose=False, force=False, extra_flags=()):
     nvcc = nvcc_path()
+    extra_flags = (*extra_flags, *os.environ.get("DMGB_NVCC_FLAGS", "").split())
     objdir = os.path.join(LIBDIR, "obj")
     os.makedirs(objdir, exist_ok=True)
+    # objects built with other flags are rebuilt
+    stamp = os.path.join(objdir, "flags.txt")
+    flags_id = " ".join([*ARCH, *NVCC_FLAGS, *extra_flags])
+    if not os.path.exists(stamp) or open(stamp).read() != flags_id:
+        force = True
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     headers.append(os.path.join(PKG, "..", "include", "dmgb.h"))
     jobs = []
@@ -84,6 +90,8 @@ def build_library(verbose=False, force=False, extra_flags=()):
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(lib + ".tmp", lib)
+    with open(stamp, "w") as fh:
+        fh.write(flags_id)
     return lib
 
 

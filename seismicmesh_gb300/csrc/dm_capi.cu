@@ -1,6 +1,7 @@
 // extern "C" entry points of libdmgb.so (declared in include/dmgb.h).
 #include "dm_common.cuh"
 #include "dm_predicates.cuh"
+#include "dm_fixed.cuh"
 
 namespace dm {
 int delaunay_workspace(int dim, int64_t n, size_t *bytes);
@@ -334,6 +335,34 @@ int dm_pad_grid(const double *src, const int32_t *n_host,
 // Debug aid (not part of the public ABI): host evaluation of the individual
 // predicate stages (0 orient3_exact, 1 orient3_slow, 2 insph3_exact,
 // 3 insph3_slow, 4 orient2_exact, 5 incirc2_exact).
+// Debug aid: fixed-point predicates on points converted at scale 2^g
+// (relative to a).  Returns -99 when a point has no exact representation.
+extern "C" int dmdbg_fixed_pred(int kind, int g, const float *a, const float *b,
+                                const float *c, const float *d, const float *e) {
+  const float *pts[4] = {b, c, d, e};
+  int4 q[4];
+  int dim = kind >= 2 ? 2 : 3;
+  int npts = kind == 0 ? 3 : kind == 1 ? 4 : kind == 2 ? 2 : 3;
+  for (int i = 0; i < npts; ++i) {
+    long long v[3] = {0, 0, 0};
+    for (int k = 0; k < dim; ++k) {
+      long long X, P;
+      if (!dmp::float_to_fixed(pts[i][k], g, &X) || !dmp::float_to_fixed(a[k], g, &P))
+        return -99;
+      v[k] = X - P;
+      if (v[k] <= -(1ll << 30) || v[k] >= (1ll << 30)) return -99;
+    }
+    q[i] = make_int4((int)v[0], (int)v[1], (int)v[2], 1);
+  }
+  switch (kind) {
+    case 0: return dmp::orient3_fx(q[0], q[1], q[2]);
+    case 1: return dmp::insph3_fx_sos(q[0], q[1], q[2], q[3]);
+    case 2: return dmp::orient2_fx(q[0], q[1]);
+    case 3: return dmp::incirc2_fx_sos(q[0], q[1], q[2]);
+  }
+  return -98;
+}
+
 extern "C" int dmdbg_host_pred(int kind, const float *a, const float *b,
                                const float *c, const float *d, const float *e) {
   int ovf = 0;

@@ -24,9 +24,11 @@
 // whose queries walk the uniform grid and its coarse blocks and are exact
 // over the whole point set.
 #include <float.h>
+#include <string.h>
 
 #include "dm_common.cuh"
 #include "dm_predicates.cuh"
+#include "dm_fixed.cuh"
 
 namespace dm {
 
@@ -67,6 +69,7 @@ struct DTArgs {
   int64_t cap_cells, cap_blocks;
   int dbg_vertex;  // debug aid: level-1 state of this vertex goes to dbg
   int32_t *dbg;
+  int dbg_full;    // debug aid: face queries always scan the whole half-space
 };
 
 static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
@@ -324,6 +327,7 @@ constexpr int L1_WARPS = 4;
 template <int DIM>
 struct WarpL1 {
   float4 c[L1<DIM>::CAP];  // relative coords (x,y,z) and lift (w)
+  int4 ci[L1<DIM>::CAP];   // exact fixed-point relative coords; w = 1 if valid
   int id[L1<DIM>::CAP];    // global index
   uint32_t tri[L1<DIM>::MAXTRI];
   uint32_t open[L1<DIM>::MAXOPEN];
@@ -361,6 +365,8 @@ __device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
   int s = dmp::orient3_rel_filter<float>(A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
                                          C.z, 16.0f * DMP_U32);
   if (s) return s;
+  const int4 IA = S.ci[a], IB = S.ci[b], IC = S.ci[c];
+  if (IA.w & IB.w & IC.w) return dmp::orient3_fx(IA, IB, IC);
   float pr[3], ar[3], br[3], cr[3];
   load_pt<3>(P, ip, pr);
   load_pt<3>(P, S.id[a], ar);
@@ -378,6 +384,8 @@ __device__ __forceinline__ int is3L(const WarpL1<3> &S, const float *P, int ip,
   int s = dmp::insph3_rel_filter<float>(X, Y, Z, Q, A.w, B.w, C.w, D.w,
                                         48.0f * DMP_U32);
   if (s) return s;
+  const int4 IA = S.ci[a], IB = S.ci[b], IC = S.ci[c], ID = S.ci[d];
+  if (IA.w & IB.w & IC.w & ID.w) return dmp::insph3_fx_sos(IA, IB, IC, ID);
   float pr[3], ar[3], br[3], cr[3], dr[3];
   load_pt<3>(P, ip, pr);
   load_pt<3>(P, S.id[a], ar);
@@ -485,6 +493,62 @@ __device__ __forceinline__ bool certified3(float4 A, float4 B, float4 C,
 // clipped by the grid need no limit).  A 16-bin histogram of d / r picks the
 // largest radius whose ball holds <= CAP points; when the first bin alone
 // overflows (dense clusters) the radius is divided by 16 and re-histogrammed.
+// Fixed-point frame: coordinates relative to p at scale 2^g, where
+// g = exponent(extent) - 28 keeps |relative coordinate| < 2^30 for points
+// within `extent` of p (per axis).  Points that are not multiples of 2^g or
+// fall outside the range get w = 0 and use the floating-point exact path.
+struct FxFrame {
+  int g;
+  bool ok;  // p itself is representable
+  long long P0[3];
+};
+
+template <int DIM>
+__device__ __forceinline__ void fx_frame(FxFrame &fr, const float *p, float extent) {
+  fr.g = dmp::float_exponent(extent) - 28;
+  fr.ok = extent > 0.f && dmp::float_exponent(extent) > -100;
+  for (int k = 0; k < 3; ++k) fr.P0[k] = 0;
+  for (int k = 0; k < DIM; ++k) fr.ok = fr.ok && dmp::float_to_fixed(p[k], fr.g, &fr.P0[k]);
+}
+
+template <int DIM>
+__device__ __forceinline__ int4 fx_point(const FxFrame &fr, const float *x) {
+  int v[3] = {0, 0, 0};
+  if (!fr.ok) return make_int4(0, 0, 0, 0);
+  for (int k = 0; k < DIM; ++k) {
+    long long X;
+    if (!dmp::float_to_fixed(x[k], fr.g, &X)) return make_int4(0, 0, 0, 0);
+    long long d = X - fr.P0[k];
+    if (d <= -(1ll << 30) || d >= (1ll << 30)) return make_int4(0, 0, 0, 0);
+    v[k] = (int)d;
+  }
+  return make_int4(v[0], v[1], v[2], 1);
+}
+
+// Exact fixed-point coordinates of the candidates relative to p: scale 2^g
+// with g chosen so that |relative coordinate| < 2^30.  A candidate (or the
+// whole star, when p itself is not a multiple of 2^g) without an exact
+// representation keeps w = 0 and uses the floating-point exact path.
+template <int DIM>
+__device__ __forceinline__ void fixed_coords(WarpL1<DIM> &S, const DTArgs &A,
+                                             const float *px, int lane) {
+  const int nc = S.nc;
+  float m = 0.f;
+  for (int j = lane; j < nc; j += 32) {
+    float4 c = S.c[j];
+    m = fmaxf(m, fmaxf(fabsf(c.x), fmaxf(fabsf(c.y), DIM == 3 ? fabsf(c.z) : 0.f)));
+  }
+  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  FxFrame fr;
+  fx_frame<DIM>(fr, px, m);
+  for (int j = lane; j < nc; j += 32) {
+    float xq[3];
+    load_pt<DIM>(A.P, S.id[j], xq);
+    S.ci[j] = fx_point<DIM>(fr, xq);
+  }
+  __syncwarp();
+}
+
 template <int DIM>
 __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const GridParams &g,
                                           int ip, const float *px, int lane, int K) {
@@ -589,6 +653,7 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
   __syncwarp();
   if (lane == 0 && S.nc > L1<DIM>::CAP) S.nc = L1<DIM>::CAP;  // cannot happen
   __syncwarp();
+  fixed_coords<DIM>(S, A, px, lane);
 }
 
 // is the cell (p, a, b, c) of a packed link triangle empty w.r.t. every
@@ -686,6 +751,8 @@ __device__ __forceinline__ int o2L(const WarpL1<2> &S, const float *P, int ip,
   float4 A = S.c[a], B = S.c[b];
   int s = dmp::orient2_rel_filter<float>(A.x, A.y, B.x, B.y, 8.0f * DMP_U32);
   if (s) return s;
+  const int4 IA = S.ci[a], IB = S.ci[b];
+  if (IA.w & IB.w) return dmp::orient2_fx(IA, IB);
   float pr[2], ar[2], br[2];
   load_pt<2>(P, ip, pr);
   load_pt<2>(P, S.id[a], ar);
@@ -701,6 +768,8 @@ __device__ __forceinline__ int ic2L(const WarpL1<2> &S, const float *P, int ip,
   float X[2] = {A.x, A.y}, Y[2] = {B.x, B.y}, Z[2] = {D.x, D.y};
   int s = dmp::incirc2_rel_filter<float>(X, Y, Z, A.w, B.w, D.w, 16.0f * DMP_U32);
   if (s) return s;
+  const int4 IA = S.ci[a], IB = S.ci[b], ID = S.ci[d];
+  if (IA.w & IB.w & ID.w) return dmp::incirc2_fx_sos(IA, IB, ID);
   float pr[2], ar[2], br[2], dr[2];
   load_pt<2>(P, ip, pr);
   load_pt<2>(P, S.id[a], ar);
@@ -1092,6 +1161,22 @@ struct GQ {
   GridParams g;
 };
 
+// Level-2 per-star statistics, compiled in only with -DDM_L2_STATS:
+// g_l2s[star] = {cycles, ntri | ip << 32, hull scans, region cells, points
+// considered, kind-1 regions, kind-2 regions, widened local searches}
+#ifdef DM_L2_STATS
+constexpr int kL2StatStars = 1 << 17, kL2StatWarps = 152 * 8 * 4;
+static __device__ unsigned long long g_l2s[kL2StatStars][8];
+static __device__ unsigned long long g_l2w[kL2StatWarps][8];
+__device__ __forceinline__ void l2s_add(int i, unsigned long long v) {
+  int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (w < kL2StatWarps) atomicAdd(&g_l2w[w][i], v);
+}
+#define L2S_ADD(i, v) l2s_add(i, v)
+#else
+#define L2S_ADD(i, v) ((void)0)
+#endif
+
 template <int DIM>
 __device__ __forceinline__ void ldp(const DTArgs &A, int i, float *x) {
   load_pt<DIM>(A.P, i, x);
@@ -1101,8 +1186,18 @@ __device__ __forceinline__ void ldp(const DTArgs &A, int i, float *x) {
 struct Face3 {
   int ip, ia, ib;
   float p[3], a[3], b[3];
-  float V[3], U[3], n[3];
+  float V[3], U[3];
+  FxFrame fr;    // fixed-point frame at p covering 8x the face size
+  int4 IA, IB;   // a, b in that frame
 };
+
+__device__ __forceinline__ void face3_frame(Face3 &F) {
+  float e = 0.f;
+  for (int k = 0; k < 3; ++k) e = fmaxf(e, fmaxf(fabsf(F.V[k]), fabsf(F.U[k])));
+  fx_frame<3>(F.fr, F.p, 8.f * e);
+  F.IA = fx_point<3>(F.fr, F.a);
+  F.IB = fx_point<3>(F.fr, F.b);
+}
 
 __device__ __forceinline__ int side3(const Face3 &F, const float *y,
                                      dmp::ExactScratch *W) {
@@ -1110,17 +1205,38 @@ __device__ __forceinline__ int side3(const Face3 &F, const float *y,
   int s = dmp::orient3_rel_filter<float>(F.V[0], F.V[1], F.V[2], F.U[0], F.U[1],
                                          F.U[2], Y[0], Y[1], Y[2], 16.0f * DMP_U32);
   if (s) return s;
+  const int4 IY = fx_point<3>(F.fr, y);
+  if (F.IA.w & F.IB.w & IY.w) return dmp::orient3_fx(F.IA, F.IB, IY);
   return dmp::orient3_slow(F.p, F.a, F.b, y, W);
+}
+
+// perturbed insph3(p, a, b, c, d) of a face query
+__device__ __forceinline__ int insph_face3(const Face3 &F, const float *c, const float *d,
+                                           int &ovf, dmp::ExactScratch *W) {
+  float Z[3] = {c[0] - F.p[0], c[1] - F.p[1], c[2] - F.p[2]};
+  float Q[3] = {d[0] - F.p[0], d[1] - F.p[1], d[2] - F.p[2]};
+  float wx = F.V[0] * F.V[0] + F.V[1] * F.V[1] + F.V[2] * F.V[2];
+  float wy = F.U[0] * F.U[0] + F.U[1] * F.U[1] + F.U[2] * F.U[2];
+  float wz = Z[0] * Z[0] + Z[1] * Z[1] + Z[2] * Z[2];
+  float wq = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2];
+  int s = dmp::insph3_rel_filter<float>(F.V, F.U, Z, Q, wx, wy, wz, wq, 48.0f * DMP_U32);
+  if (s) return s;
+  const int4 IC = fx_point<3>(F.fr, c), ID = fx_point<3>(F.fr, d);
+  if (F.IA.w & F.IB.w & IC.w & ID.w) return dmp::insph3_fx_sos(F.IA, F.IB, IC, ID);
+  s = dmp::insph3_slow(F.p, F.a, F.b, c, d, &ovf, W);
+  if (s) return s;
+  return dmp::insph3_sos_tail(F.p, F.a, F.b, c, d, W);
 }
 
 __device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j,
                                           int &best, float *bx, int &ovf,
                                           dmp::ExactScratch *W) {
   if (j == F.ip || j == F.ia || j == F.ib || A.dup[j]) return;
+  L2S_ADD(3, 1);
   float y[3];
   load_pt<3>(A.P, j, y);
   if (side3(F, y, W) <= 0) return;
-  if (best < 0 || insph3_sos(F.p, F.a, F.b, bx, y, &ovf, W) < 0) {
+  if (best < 0 || insph_face3(F, bx, y, ovf, W) < 0) {
     best = j;
     bx[0] = y[0];
     bx[1] = y[1];
@@ -1140,7 +1256,7 @@ __device__ __forceinline__ int tourney3(const DTArgs &A, const Face3 &F,
         float bx[3], ox[3];
         load_pt<3>(A.P, best, bx);
         load_pt<3>(A.P, other, ox);
-        if (insph3_sos(F.p, F.a, F.b, bx, ox, &ovf, W) < 0) best = other;
+        if (insph_face3(F, bx, ox, ovf, W) < 0) best = other;
       }
     }
   }
@@ -1152,10 +1268,174 @@ __device__ __forceinline__ bool in_local(const int *cc, int x, int y, int z,
   return abs(x - cc[0]) <= 1 && abs(y - cc[1]) <= 1 && (dim == 2 || abs(z - cc[2]) <= 1);
 }
 
+// cells [lo, hi] on axis k covering [c - r, c + r], padded by one cell and
+// clipped to the grid (computed in double: r may be huge); lo > hi when the
+// interval misses the grid
+__device__ __forceinline__ void cell_range(const GridParams &g, double c, double r,
+                                           int k, int &lo, int &hi) {
+  double a = floor((c - r - g.lo[k]) * g.inv_cs) - 1;
+  double b = floor((c + r - g.lo[k]) * g.inv_cs) + 1;
+  lo = (int)fmax(0.0, fmin(a, (double)g.dims[k]));
+  hi = (int)fmin((double)(g.dims[k] - 1), fmax(b, -1.0));
+}
+
 // the points of cell c
 template <typename F>
 __device__ __forceinline__ void for_cell(const DTArgs &A, int c, F f) {
   for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) f(A.sorted[i]);
+}
+
+// Search region of a gift-wrap query on face (p, a, b) with current winner y:
+// every point that beats y lies in sphere(p, a, b, y) on the positive side
+// H+ of the face.  Kinds:
+//  1: the face circumcircle (cc, r) is well conditioned.  With z(x) the
+//     height over the face, the region is {x in H+ : |x-cc|^2 - r^2 <= 2 Z z(x)}
+//     for any Z >= z0 (the sphere centre's height).  Z < 0 gives a thin lens.
+//  2: ill-conditioned face, well-conditioned tetrahedron: the circumsphere
+//     (s, R) of (p, a, b, y) intersected with H+.
+//  0: neither: all of H+ (culling only by the face plane when its normal is
+//     resolvable).
+struct Region3 {
+  int kind;
+  bool cull;          // the unit normal un is accurate (plane culling allowed)
+  double p[3], un[3];
+  double cc[3], r2, Z, dcc;  // kind 1 (cc absolute), dcc: error bound of cc
+  double s[3], R2;           // kind 2
+  double lo[3], hi[3];       // bounding box of the region (kinds 1, 2)
+};
+
+// double-precision region from the exact face/winner differences
+__device__ __forceinline__ void make_region3(Region3 &R, const float *fp, const double *a,
+                                             const double *b, const double *n, double nn,
+                                             double la, double lb, const float *y) {
+  const double u = 1.2e-16;
+  for (int k = 0; k < 3; ++k) R.p[k] = fp[k];
+  R.cull = nn > 1e-20 * la * lb;
+  const double inl = R.cull ? 1.0 / sqrt(nn) : 0.0;
+  for (int k = 0; k < 3; ++k) R.un[k] = n[k] * inl;
+  R.kind = 0;
+  if (!y) return;
+  double c[3];
+  for (int k = 0; k < 3; ++k) c[k] = (double)y[k] - fp[k];
+  if (nn > 1e-12 * la * lb) {
+    // |dn| <= 4u|a||b|; |dcc| <= 16u (la|b| + lb|a|)|a||b| / nn + 1e-9 r
+    double al = sqrt(la), bl = sqrt(lb), nl = sqrt(nn);
+    double t[3] = {la * b[0] - lb * a[0], la * b[1] - lb * a[1], la * b[2] - lb * a[2]};
+    double inv = 0.5 / nn;
+    double cc[3] = {(t[1] * n[2] - t[2] * n[1]) * inv, (t[2] * n[0] - t[0] * n[2]) * inv,
+                    (t[0] * n[1] - t[1] * n[0]) * inv};
+    double r2 = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2];
+    double r = sqrt(r2);
+    double dcc = 16 * u * (la * bl + lb * al) * al * bl / nn + 1e-9 * r;
+    double w[3] = {c[0] - cc[0], c[1] - cc[1], c[2] - cc[2]};
+    double lw = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    double q = lw - r2;
+    double eq = 4 * (sqrt(lw) + r + dcc) * dcc + 1e-14 * (lw + r2);
+    double lc = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    double hgt = (c[0] * n[0] + c[1] * n[1] + c[2] * n[2]) / nl;  // > 0 exactly
+    double dh = 2 * lc * u * (4 * al * bl / nl + 3);
+    double Z;
+    bool ok = true;
+    if (q + eq <= 0) {
+      Z = (q + eq) / (2 * (hgt + dh));  // <= 0: an upper bound of z0
+    } else if (hgt > 2 * dh) {
+      Z = (q + eq) / (2 * (hgt - dh));
+    } else {
+      ok = false;
+    }
+    if (ok && Z < 1e30) {
+      R.kind = 1;
+      for (int k = 0; k < 3; ++k) R.cc[k] = cc[k] + fp[k];
+      R.r2 = r2;
+      R.Z = Z;
+      R.dcc = dcc + 1e-7 * (fabs(R.cc[0]) + fabs(R.cc[1]) + fabs(R.cc[2]));
+      // the region lies in B(cc, r) when Z <= 0, else in the sphere itself
+      double ctr[3], rb;
+      if (Z <= 0) {
+        for (int k = 0; k < 3; ++k) ctr[k] = R.cc[k];
+        rb = r;
+      } else {
+        for (int k = 0; k < 3; ++k) ctr[k] = R.cc[k] + Z * n[k] / nl;
+        rb = sqrt(r2 + Z * Z);
+      }
+      rb = rb * (1 + 1e-6) + R.dcc;
+      for (int k = 0; k < 3; ++k) {
+        R.lo[k] = ctr[k] - rb;
+        R.hi[k] = ctr[k] + rb;
+      }
+      return;
+    }
+  }
+  // circumsphere of the tetrahedron (p, a, b, y)
+  double bc[3] = {b[1] * c[2] - b[2] * c[1], b[2] * c[0] - b[0] * c[2],
+                  b[0] * c[1] - b[1] * c[0]};
+  double ca[3] = {c[1] * a[2] - c[2] * a[1], c[2] * a[0] - c[0] * a[2],
+                  c[0] * a[1] - c[1] * a[0]};
+  double det = a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2];
+  double perm = fabs(a[0]) * (fabs(b[1] * c[2]) + fabs(b[2] * c[1])) +
+                fabs(a[1]) * (fabs(b[2] * c[0]) + fabs(b[0] * c[2])) +
+                fabs(a[2]) * (fabs(b[0] * c[1]) + fabs(b[1] * c[0]));
+  if (fabs(det) > 1e-9 * perm) {
+    double lc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+    double s[3];
+    for (int k = 0; k < 3; ++k) s[k] = (la * bc[k] + lb * ca[k] + lc * n[k]) / (2 * det);
+    double rad = sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    for (int k = 0; k < 3; ++k) s[k] += fp[k];
+    rad = rad * (1 + 1e-6) + 1e-7 * (fabs(s[0]) + fabs(s[1]) + fabs(s[2]));
+    if (rad < 1e30) {
+      R.kind = 2;
+      R.R2 = rad * rad;
+      for (int k = 0; k < 3; ++k) {
+        R.s[k] = s[k];
+        R.lo[k] = s[k] - rad;
+        R.hi[k] = s[k] + rad;
+      }
+    }
+  }
+}
+
+// may the box [lo, hi] hold a point of the region?  (conservative)
+__device__ __forceinline__ bool region_hits3(const Region3 &R, const float *lo,
+                                             const float *hi) {
+  // heights of the box corners over the face plane, and distance bounds
+  double zmin = 1e300, zmax = -1e300, dp2 = 0;
+  for (int corner = 0; corner < 8; ++corner) {
+    double z = 0, d2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      double v = (double)((corner >> k) & 1 ? hi[k] : lo[k]) - R.p[k];
+      z += v * R.un[k];
+      d2 += v * v;
+    }
+    zmin = fmin(zmin, z);
+    zmax = fmax(zmax, z);
+    dp2 = fmax(dp2, d2);
+  }
+  const double dp = sqrt(dp2);
+  if (R.cull && zmax < -1e-5 * dp) return false;  // entirely below the face
+  if (R.kind == 0) return true;
+  if (R.kind == 2) {
+    double d2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      double e = fmax(fmax((double)lo[k] - R.s[k], R.s[k] - (double)hi[k]), 0.0);
+      d2 += e * e;
+    }
+    return d2 <= R.R2 * (1 + 1e-9) + 1e-30;
+  }
+  // kind 1: lower bound of |x-cc|^2 - 2 Z z(x) - r^2 over the box within H+
+  double d2 = 0;
+  for (int k = 0; k < 3; ++k) {
+    double e = fmax(fmax((double)lo[k] - R.cc[k], R.cc[k] - (double)hi[k]), 0.0);
+    d2 += e * e;
+  }
+  double zb = R.Z > 0 ? zmax : fmax(zmin, 0.0);
+  double gl = d2 - 2 * R.Z * zb - R.r2;
+  double tol = 2 * dp * R.dcc + 1e-9 * (d2 + R.r2 + fabs(2 * R.Z * zb)) + 1e-8 * dp * fabs(2 * R.Z);
+  return gl <= tol;
+}
+
+// Chebyshev distance of cell (x, y, z) from cell cc
+__device__ __forceinline__ int cheb3(const int *cc, int x, int y, int z) {
+  return max(abs(x - cc[0]), max(abs(y - cc[1]), abs(z - cc[2])));
 }
 
 // exhaustive gift-wrap query on face (p, a, b), 3D
@@ -1173,78 +1453,76 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     F.V[k] = F.a[k] - F.p[k];
     F.U[k] = F.b[k] - F.p[k];
   }
-  F.n[0] = F.V[1] * F.U[2] - F.V[2] * F.U[1];
-  F.n[1] = F.V[2] * F.U[0] - F.V[0] * F.U[2];
-  F.n[2] = F.V[0] * F.U[1] - F.V[1] * F.U[0];
+  face3_frame(F);
+  // face normal from the exact differences
+  double a[3], b[3];
+  for (int k = 0; k < 3; ++k) {
+    a[k] = (double)F.a[k] - F.p[k];
+    b[k] = (double)F.b[k] - F.p[k];
+  }
+  const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                       a[0] * b[1] - a[1] * b[0]};
+  const double nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+  const double la = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+  const double lb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
   int best = -1;
   float bx[3];
   int cc[3];
   for (int k = 0; k < 3; ++k)
     cc[k] = cell_coord(g, (F.p[k] + F.a[k] + F.b[k]) * (1.f / 3.f), k);
-  if (lane < 27) {
-    int x = cc[0] + lane % 3 - 1, y = cc[1] + (lane / 3) % 3 - 1,
-        z = cc[2] + lane / 9 - 1;
+  auto scan_cell = [&](int x, int y, int z) {
     if (x >= 0 && y >= 0 && z >= 0 && x < g.dims[0] && y < g.dims[1] && z < g.dims[2])
       for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
                [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
-  }
+  };
+  // local search: the 27 cells around the face centroid
+  if (lane < 27) scan_cell(cc[0] + lane % 3 - 1, cc[1] + (lane / 3) % 3 - 1, cc[2] + lane / 9 - 1);
+  // after a tournament every lane holds the same winner: reload its point
   best = tourney3(A, F, best, ovf, W);
-  // search region
-  bool full = true;
-  double cen[3] = {0, 0, 0}, rad = 0;
-  if (best >= 0) {
-    load_pt<3>(A.P, best, bx);
-    double a[3], b[3], c[3];
-    for (int k = 0; k < 3; ++k) {
-      a[k] = (double)F.a[k] - F.p[k];
-      b[k] = (double)F.b[k] - F.p[k];
-      c[k] = (double)bx[k] - F.p[k];
+  if (best >= 0) load_pt<3>(A.P, best, bx);
+  Region3 R;
+  make_region3(R, F.p, a, b, n, nn, la, lb, best >= 0 ? bx : nullptr);
+  int rex = 1;  // cells with Chebyshev distance <= rex are done
+  // a large region: widen the local search to the 5^3 cells first
+  bool large = R.kind == 0;
+  for (int k = 0; k < 3 && !large; ++k)
+    large = (R.hi[k] - R.lo[k]) * g.inv_cs > 5.0;
+  if (large) {
+    for (int t = lane; t < 125; t += 32) {
+      int dx = t % 5 - 2, dy = (t / 5) % 5 - 2, dz = t / 25 - 2;
+      if (max(abs(dx), max(abs(dy), abs(dz))) == 2) scan_cell(cc[0] + dx, cc[1] + dy, cc[2] + dz);
     }
-    double bc[3] = {b[1] * c[2] - b[2] * c[1], b[2] * c[0] - b[0] * c[2],
-                    b[0] * c[1] - b[1] * c[0]};
-    double ca[3] = {c[1] * a[2] - c[2] * a[1], c[2] * a[0] - c[0] * a[2],
-                    c[0] * a[1] - c[1] * a[0]};
-    double ab[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
-                    a[0] * b[1] - a[1] * b[0]};
-    double det = a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2];
-    double perm = fabs(a[0]) * (fabs(b[1] * c[2]) + fabs(b[2] * c[1])) +
-                  fabs(a[1]) * (fabs(b[2] * c[0]) + fabs(b[0] * c[2])) +
-                  fabs(a[2]) * (fabs(b[0] * c[1]) + fabs(b[1] * c[0]));
-    if (fabs(det) > 1e-9 * perm) {
-      double la = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
-      double lb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
-      double lc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-      for (int k = 0; k < 3; ++k) cen[k] = (la * bc[k] + lb * ca[k] + lc * ab[k]) / (2 * det);
-      rad = sqrt(cen[0] * cen[0] + cen[1] * cen[1] + cen[2] * cen[2]);
-      for (int k = 0; k < 3; ++k) cen[k] += F.p[k];
-      rad = rad * (1 + 1e-6) + 1e-7 * (fabs(cen[0]) + fabs(cen[1]) + fabs(cen[2]));
-      full = false;
-    }
+    best = tourney3(A, F, best, ovf, W);
+    rex = 2;
+    if (best >= 0) load_pt<3>(A.P, best, bx);
+    make_region3(R, F.p, a, b, n, nn, la, lb, best >= 0 ? bx : nullptr);
   }
-  if (!full) {
+  if (A.dbg_full) {
+    R.kind = 0;
+    rex = 1;
+  }
+  if (lane == 0) {
+    if (R.kind == 1) L2S_ADD(4, 1);
+    if (R.kind == 2) L2S_ADD(5, 1);
+    if (large) L2S_ADD(6, 1);
+  }
+  if (R.kind != 0) {
     int lo[3], hi[3];
     int64_t ncell = 1;
     for (int k = 0; k < 3; ++k) {
-      lo[k] = max(0, (int)floor((cen[k] - rad - g.lo[k]) * g.inv_cs) - 1);
-      hi[k] = min(g.dims[k] - 1, (int)floor((cen[k] + rad - g.lo[k]) * g.inv_cs) + 1);
-      ncell *= (hi[k] - lo[k] + 1);
+      double c0 = 0.5 * (R.lo[k] + R.hi[k]), r0 = 0.5 * (R.hi[k] - R.lo[k]);
+      cell_range(g, c0, r0, k, lo[k], hi[k]);
+      ncell *= max(0, hi[k] - lo[k] + 1);
     }
-    float r2 = (float)(rad * rad) * 1.0001f;
+    if (lane == 0) L2S_ADD(2, ncell);
     if (ncell <= 4096) {
       int sx = hi[0] - lo[0] + 1, sy = hi[1] - lo[1] + 1;
       for (int t = lane; t < ncell; t += 32) {
         int x = lo[0] + t % sx, y = lo[1] + (t / sx) % sy, z = lo[2] + t / (sx * sy);
-        if (in_local(cc, x, y, z, 3)) continue;
-        // cell box vs sphere
-        float dd = 0.f;
-        int ci[3] = {x, y, z};
-        for (int k = 0; k < 3; ++k) {
-          float b0 = g.lo[k] + ci[k] * g.cs, b1 = b0 + g.cs;
-          float c = (float)cen[k];
-          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
-          dd += e * e;
-        }
-        if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
+        if (cheb3(cc, x, y, z) <= rex) continue;
+        float blo[3] = {g.lo[0] + x * g.cs, g.lo[1] + y * g.cs, g.lo[2] + z * g.cs};
+        float bhi[3] = {blo[0] + g.cs, blo[1] + g.cs, blo[2] + g.cs};
+        if (!region_hits3(R, blo, bhi)) continue;
         for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
                  [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
       }
@@ -1262,18 +1540,11 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
             bzi = blo[2] + (int)(t / (sx * sy));
         int bid = bxi + g.bdims[0] * (byi + g.bdims[1] * bzi);
         if (A.blk_cnt[bid] == 0) continue;
-        float dd = 0.f;
-        for (int k = 0; k < 3; ++k) {
-          float b0 = A.blk_box[6 * bid + k], b1 = A.blk_box[6 * bid + 3 + k];
-          float c = (float)cen[k];
-          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
-          dd += e * e;
-        }
-        if (dd > r2 * 1.0001f + 1e-6f * g.cs * g.cs) continue;
+        if (!region_hits3(R, A.blk_box + 6 * bid, A.blk_box + 6 * bid + 3)) continue;
         for (int z = bzi * g.bs; z < min(bzi * g.bs + g.bs, g.dims[2]); ++z)
           for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
             for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
-              if (in_local(cc, x, y, z, 3)) continue;
+              if (cheb3(cc, x, y, z) <= rex) continue;
               for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
                        [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
             }
@@ -1281,26 +1552,16 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     }
   } else {
     // every block that may hold a point on the positive side
-    float nrm = sqrtf(F.n[0] * F.n[0] + F.n[1] * F.n[1] + F.n[2] * F.n[2]);
+    if (lane == 0) L2S_ADD(1, 1);
     for (int bid = lane; bid < g.nblocks; bid += 32) {
       if (A.blk_cnt[bid] == 0) continue;
-      float mx = -FLT_MAX, scale = 0.f;
-      for (int corner = 0; corner < 8; ++corner) {
-        float d = 0.f;
-        for (int k = 0; k < 3; ++k) {
-          float v = A.blk_box[6 * bid + ((corner >> k) & 1) * 3 + k] - F.p[k];
-          d += v * F.n[k];
-          scale = fmaxf(scale, fabsf(v));
-        }
-        mx = fmaxf(mx, d);
-      }
-      if (mx < -1e-4f * nrm * scale) continue;
+      if (!region_hits3(R, A.blk_box + 6 * bid, A.blk_box + 6 * bid + 3)) continue;
       int bxi = bid % g.bdims[0], byi = (bid / g.bdims[0]) % g.bdims[1],
           bzi = bid / (g.bdims[0] * g.bdims[1]);
       for (int z = bzi * g.bs; z < min(bzi * g.bs + g.bs, g.dims[2]); ++z)
         for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
           for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
-            if (in_local(cc, x, y, z, 3)) continue;
+            if (cheb3(cc, x, y, z) <= rex) continue;
             for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
                      [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
           }
@@ -1315,22 +1576,48 @@ struct Edge2 {
   int ip, ix, sgn;
   float p[2], x[2];
   float X[2];
+  FxFrame fr;  // fixed-point frame at p covering 8x the edge length
+  int4 IX;
 };
+
+__device__ __forceinline__ void edge2_frame(Edge2 &E) {
+  fx_frame<2>(E.fr, E.p, 8.f * fmaxf(fabsf(E.X[0]), fabsf(E.X[1])));
+  E.IX = fx_point<2>(E.fr, E.x);
+}
 
 __device__ __forceinline__ int side2(const Edge2 &E, const float *y,
                                      dmp::ExactScratch *W) {
   float Y[2] = {y[0] - E.p[0], y[1] - E.p[1]};
   int s = dmp::orient2_rel_filter<float>(E.X[0], E.X[1], Y[0], Y[1], 8.0f * DMP_U32);
-  if (!s) s = dmp::orient2_slow(E.p, E.x, y, W);
+  if (!s) {
+    const int4 IY = fx_point<2>(E.fr, y);
+    s = (E.IX.w & IY.w) ? dmp::orient2_fx(E.IX, IY) : dmp::orient2_slow(E.p, E.x, y, W);
+  }
   return s * E.sgn;
+}
+
+// perturbed incirc2(p, b, c, d) of an edge query
+__device__ __forceinline__ int incirc_edge2(const Edge2 &E, const float *b, const float *c,
+                                            const float *d, int &ovf, dmp::ExactScratch *W) {
+  float X[2] = {b[0] - E.p[0], b[1] - E.p[1]}, Y[2] = {c[0] - E.p[0], c[1] - E.p[1]},
+        Z[2] = {d[0] - E.p[0], d[1] - E.p[1]};
+  int s = dmp::incirc2_rel_filter<float>(X, Y, Z, X[0] * X[0] + X[1] * X[1],
+                                         Y[0] * Y[0] + Y[1] * Y[1], Z[0] * Z[0] + Z[1] * Z[1],
+                                         16.0f * DMP_U32);
+  if (s) return s;
+  const int4 IB = fx_point<2>(E.fr, b), IC = fx_point<2>(E.fr, c), ID = fx_point<2>(E.fr, d);
+  if (IB.w & IC.w & ID.w) return dmp::incirc2_fx_sos(IB, IC, ID);
+  s = dmp::incirc2_slow(E.p, b, c, d, &ovf, W);
+  if (s) return s;
+  return dmp::incirc2_sos_tail(E.p, b, c, d, W);
 }
 
 __device__ __forceinline__ int cmp2(const Edge2 &E, const float *bx,
                                     const float *y, int &ovf,
                                     dmp::ExactScratch *W) {
   // <0 when y lies inside the circle of the current triangle
-  return E.sgn > 0 ? incirc2_sos(E.p, E.x, bx, y, &ovf, W)
-                   : incirc2_sos(E.p, bx, E.x, y, &ovf, W);
+  return E.sgn > 0 ? incirc_edge2(E, E.x, bx, y, ovf, W)
+                   : incirc_edge2(E, bx, E.x, y, ovf, W);
 }
 
 __device__ __forceinline__ void consider2(const DTArgs &A, const Edge2 &E, int j,
@@ -1377,6 +1664,7 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
   load_pt<2>(A.P, ix, E.x);
   E.X[0] = E.x[0] - E.p[0];
   E.X[1] = E.x[1] - E.p[1];
+  edge2_frame(E);
   int best = -1;
   float bx[2];
   int cc[3] = {cell_coord(g, 0.5f * (E.p[0] + E.x[0]), 0),
@@ -1387,34 +1675,53 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
       for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
   }
   best = tourney2(A, E, best, ovf, W);
+  // Search region (as in gq3): a point beating the winner y lies inside
+  // circle(p, x, y) on the positive side of the edge, which lies inside
+  // B(m + Z n^, sqrt(r^2 + Z^2)) with m, r the midpoint and half length of
+  // the edge and Z >= max(z0, 0), z0 = (|y - m|^2 - r^2) / (2 h).
   bool full = true;
   double cen[2] = {0, 0}, rad = 0;
   if (best >= 0) {
     load_pt<2>(A.P, best, bx);
+    const double u = 1.2e-16;
     double a[2] = {(double)E.x[0] - E.p[0], (double)E.x[1] - E.p[1]};
-    double b[2] = {(double)bx[0] - E.p[0], (double)bx[1] - E.p[1]};
-    double det = a[0] * b[1] - a[1] * b[0];
-    double perm = fabs(a[0] * b[1]) + fabs(a[1] * b[0]);
-    if (fabs(det) > 1e-9 * perm) {
-      double la = a[0] * a[0] + a[1] * a[1], lb = b[0] * b[0] + b[1] * b[1];
-      cen[0] = (b[1] * la - a[1] * lb) / (2 * det);
-      cen[1] = (a[0] * lb - b[0] * la) / (2 * det);
-      rad = sqrt(cen[0] * cen[0] + cen[1] * cen[1]);
-      cen[0] += E.p[0];
-      cen[1] += E.p[1];
-      rad = rad * (1 + 1e-6) + 1e-7 * (fabs(cen[0]) + fabs(cen[1]));
-      full = false;
+    double c[2] = {(double)bx[0] - E.p[0], (double)bx[1] - E.p[1]};
+    double la = a[0] * a[0] + a[1] * a[1];
+    if (la > 0) {
+      double al = sqrt(la);
+      double r2 = 0.25 * la;
+      double w[2] = {c[0] - 0.5 * a[0], c[1] - 0.5 * a[1]};
+      double lw = w[0] * w[0] + w[1] * w[1];
+      double q = lw - r2;
+      double eq = 1e-14 * (lw + r2 + la);
+      double lc = sqrt(c[0] * c[0] + c[1] * c[1]);
+      double hgt = E.sgn * (a[0] * c[1] - a[1] * c[0]) / al;
+      double dh = 8 * u * lc;
+      double Z = -1;
+      if (q + eq <= 0) {
+        Z = 0;
+      } else if (hgt > 2 * dh) {
+        Z = (q + eq) / (2 * (hgt - dh));
+      }
+      if (Z >= 0 && Z < 1e30) {
+        double nx = -E.sgn * a[1] / al, ny = E.sgn * a[0] / al;
+        cen[0] = 0.5 * a[0] + Z * nx + E.p[0];
+        cen[1] = 0.5 * a[1] + Z * ny + E.p[1];
+        rad = sqrt(r2 + Z * Z);
+        rad = rad * (1 + 1e-6) + 1e-7 * (fabs(cen[0]) + fabs(cen[1]));
+        full = !(rad < 1e30);
+      }
     }
   }
   if (!full) {
     int lo[2], hi[2];
     int64_t ncell = 1;
     for (int k = 0; k < 2; ++k) {
-      lo[k] = max(0, (int)floor((cen[k] - rad - g.lo[k]) * g.inv_cs) - 1);
-      hi[k] = min(g.dims[k] - 1, (int)floor((cen[k] + rad - g.lo[k]) * g.inv_cs) + 1);
-      ncell *= (hi[k] - lo[k] + 1);
+      cell_range(g, cen[k], rad, k, lo[k], hi[k]);
+      ncell *= max(0, hi[k] - lo[k] + 1);
     }
     float r2 = (float)(rad * rad) * 1.0001f;
+    if (lane == 0) L2S_ADD(2, ncell);
     if (ncell <= 4096) {
       int sx = hi[0] - lo[0] + 1;
       for (int t = lane; t < ncell; t += 32) {
@@ -1517,9 +1824,8 @@ __device__ __forceinline__ bool gempty(const DTArgs &A, const GridParams &g, int
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
   int64_t ncell = 1;
   for (int k = 0; k < DIM; ++k) {
-    lo[k] = max(0, (int)floor((cen[k] - rad - g.lo[k]) * g.inv_cs) - 1);
-    hi[k] = min(g.dims[k] - 1, (int)floor((cen[k] + rad - g.lo[k]) * g.inv_cs) + 1);
-    ncell *= (hi[k] - lo[k] + 1);
+    cell_range(g, cen[k], rad, k, lo[k], hi[k]);
+    ncell *= max(0, hi[k] - lo[k] + 1);
   }
   const float r2 = (float)(rad * rad) * 1.0001f;
   const int sx = hi[0] - lo[0] + 1, sy = hi[1] - lo[1] + 1;
@@ -1781,6 +2087,11 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
     int4 sd = A.esc_seed[k];
     const int ip = sd.x & ~(1 << 30);
     const bool certified = (sd.x >> 30) & 1;
+#ifdef DM_L2_STATS
+    long long t_start = clock64();
+    if (lane < 8) g_l2w[blockIdx.x * L2_WARPS + w][lane] = 0;
+    __syncwarp();
+#endif
     int ovf = 0;
     int3 seed = make_int3(-1, -1, -1);
     if (certified) {
@@ -1841,7 +2152,33 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
       A.counters[9] = S.ntri;
       A.counters[10] = S.nopen;
     }
+    if (ip == A.dbg_vertex && A.dbg) {
+      // level-2 walk of the watched vertex: [1000] ntri, [1001] certified
+      // seed flag, [1002..1004] seed, [1008 + 3t ..] triangles in walk order
+      __syncwarp();
+      if (lane == 0) {
+        A.dbg[1000] = S.ntri;
+        A.dbg[1001] = certified;
+        A.dbg[1002] = seed.x;
+        A.dbg[1003] = seed.y;
+        A.dbg[1004] = seed.z;
+      }
+      for (int t = lane; t < S.ntri; t += 32) {
+        A.dbg[1008 + 3 * t] = S.tri[t].x;
+        A.dbg[1008 + 3 * t + 1] = S.tri[t].y;
+        A.dbg[1008 + 3 * t + 2] = S.tri[t].z;
+      }
+      __syncwarp();
+    }
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+#ifdef DM_L2_STATS
+    __syncwarp();
+    if (lane == 0 && k < kL2StatStars) {
+      g_l2s[k][0] = clock64() - t_start;
+      g_l2s[k][1] = S.ntri | ((unsigned long long)ip << 32);
+      for (int q = 1; q < 7; ++q) g_l2s[k][q + 1] = g_l2w[blockIdx.x * L2_WARPS + w][q];
+    }
+#endif
     for (int t0 = 0; t0 < S.ntri; t0 += 32) {
       int t = t0 + lane;
       bool own = false;
@@ -2007,6 +2344,7 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   DM_ARG_CHECK(((uintptr_t)cells & 15) == 0, "cells misaligned");
   Carve c(ws, ws_bytes);
   DTArgs a;
+  memset(&a, 0, sizeof(a));
   carve_dt(c, a, dim, n);
   if (!c.ok() || ws == nullptr) {
     set_error("delaunay: workspace %zu < required %zu", ws_bytes, c.used);
@@ -2091,16 +2429,29 @@ __global__ void k_debug_gq(DTArgs A, const int32_t *faces, int m, int32_t *out) 
 }
 }  // namespace dm
 
+extern "C" int dmdbg_face_query_mode(int32_t dim, const float *pts, int64_t n,
+                                     void *ws, size_t ws_bytes, const int32_t *faces,
+                                     int32_t m, int32_t *out, void *stream, int32_t mode);
 extern "C" int dmdbg_face_query(int32_t dim, const float *pts, int64_t n,
                                 void *ws, size_t ws_bytes, const int32_t *faces,
                                 int32_t m, int32_t *out, void *stream) {
+  return dmdbg_face_query_mode(dim, pts, n, ws, ws_bytes, faces, m, out, stream, 0);
+}
+
+// mode 1: exhaustive half-space scan for every face (ground truth, 3D)
+extern "C" int dmdbg_face_query_mode(int32_t dim, const float *pts, int64_t n,
+                                     void *ws, size_t ws_bytes, const int32_t *faces,
+                                     int32_t m, int32_t *out, void *stream, int32_t mode) {
   using namespace dm;
   Carve c(ws, ws_bytes);
   DTArgs a;
+  memset(&a, 0, sizeof(a));
   carve_dt(c, a, dim, n);
   a.dim = dim;
   a.n = n;
   a.P = pts;
+  a.dbg_vertex = -1;
+  a.dbg_full = mode;
   k_debug_gq<<<(m + 3) / 4, 128, 0, (cudaStream_t)stream>>>(a, faces, m, out);
   DM_LAUNCH_CHECK();
   return DM_OK;
@@ -2220,4 +2571,18 @@ extern "C" int dmprof_slow_counters(unsigned long long *out8) {
   unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   cudaMemcpyToSymbol(dmp::g_slow, z, sizeof(z));
   return 0;
+}
+
+// Debug aid: copy level-2 statistics of the last dm_delaunay (stars < 2^17,
+// 8 values each); returns 0 when the statistics are not compiled in.
+extern "C" int dmprof_l2_stats(unsigned long long *out, int64_t nstars) {
+#ifdef DM_L2_STATS
+  if (nstars > dm::kL2StatStars) nstars = dm::kL2StatStars;
+  cudaMemcpyFromSymbol(out, dm::g_l2s, sizeof(unsigned long long) * 8 * nstars);
+  return 1;
+#else
+  (void)out;
+  (void)nstars;
+  return 0;
+#endif
 }

@@ -362,7 +362,8 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_max_reduce(float *maxf, int nblk) {
+// maximum of the nblk block maxima, written to maxf[slot]
+__global__ void k_max_reduce(float *maxf, int nblk, int slot) {
   __shared__ float r[1024];
   float m = 0.f;
   for (int i = threadIdx.x; i < nblk; i += blockDim.x) m = fmaxf(m, maxf[i]);
@@ -372,7 +373,7 @@ __global__ void k_max_reduce(float *maxf, int nblk) {
     if (threadIdx.x < s) r[threadIdx.x] = fmaxf(r[threadIdx.x], r[threadIdx.x + s]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) maxf[nblk] = r[0];
+  if (threadIdx.x == 0) maxf[slot] = r[0];
 }
 
 template <int DIM>
@@ -723,7 +724,10 @@ int update_points(int dim, const float *P, float *Pout, int64_t n,
   else
     k_update<2><<<nblk, 256, 0, s>>>(P, Pout, n, adj, adj_cap, deg, d, partials,
                                      nblk, L0mult, dt, nfix, L, hmin, deps, maxf);
-  k_max_reduce<<<1, 1024, 0, s>>>(maxf, nblk);
+  // the result goes to maxf[dm_bar_blocks(n)], the slot callers size
+  // (and read) independently of the dimension
+  const int slot = max(bar_blocks(2, n), bar_blocks(3, n));
+  k_max_reduce<<<1, 1024, 0, s>>>(maxf, nblk, slot);
   DM_LAUNCH_CHECK();
   note_launches(2);
   return DM_OK;

@@ -102,6 +102,57 @@ def test_host_predicates_exact_against_rationals():
     assert degenerate == 0
 
 
+def test_fixed_point_predicates_match_expansion_predicates():
+    """The integer (fixed-point) predicates used inside vertex stars give the
+    same exact, symbolically perturbed signs as the expansion predicates."""
+    import ctypes
+    import math
+
+    L = N.lib()
+    fp = N.fptr
+    f = L.dmdbg_fixed_pred
+    f.argtypes = [ctypes.c_int, ctypes.c_int] + [N._FP] * 5
+    rng = np.random.default_rng(11)
+    checked = {0: 0, 1: 0, 2: 0, 3: 0}
+    zeros = 0
+    for t in range(3000):
+        mode = t % 3
+        if mode == 0:  # small lattice: coplanar and cospherical ties
+            P = (0.3 + rng.integers(-3, 4, (5, 3)) * 0.0625).astype(np.float32)
+        elif mode == 1:  # generic points near 0.5
+            P = (0.5 + 0.05 * rng.standard_normal((5, 3))).astype(np.float32)
+        else:  # rounded lattice: ties broken by float rounding
+            P = (0.71 + rng.integers(-2, 3, (5, 3)) * 0.02).astype(np.float32)
+        if len({tuple(q) for q in P}) < 5:
+            continue
+        rel = (P[1:] - P[0]).astype(np.float32)
+        g = math.frexp(float(np.abs(rel).max()))[1] - 1 - 28
+        o = L.dm_orient3(*[fp(q) for q in P[:4]])
+        r = f(0, g, *[fp(q) for q in P])
+        if r != -99:
+            assert r == o
+            checked[0] += 1
+            zeros += o == 0
+        if o != 0:
+            r = f(1, g, *[fp(q) for q in P])
+            if r != -99:
+                assert r == L.dm_insphere_sos(*[fp(q) for q in P])
+                checked[1] += 1
+        Q = [np.ascontiguousarray(q[:2]) for q in P[:4]]
+        o2 = L.dm_orient2(*[fp(q) for q in Q[:3]])
+        r = f(2, g, *[fp(q) for q in Q], fp(Q[0]))
+        if r != -99:
+            assert r == o2
+            checked[2] += 1
+        if o2 != 0 and len({tuple(q) for q in Q}) == 4:
+            r = f(3, g, *[fp(q) for q in Q], fp(Q[0]))
+            if r != -99:
+                assert r == L.dm_incircle_sos(*[fp(q) for q in Q])
+                checked[3] += 1
+    assert min(checked.values()) > 500, checked
+    assert zeros > 20
+
+
 def test_sdf_program_encoding():
     import seismicmesh_gb300 as sm
 

@@ -90,3 +90,62 @@ def test_duplicate_points_are_merged_like_cgal(cuda):
     nc = eng.triangulate()
     assert eng.n == 500
     dc.assert_same_triangulation(eng.P[:, :3].double().cpu().numpy(), eng.cells[:nc].cpu().numpy())
+
+
+def _face_queries(P, faces, mode):
+    import ctypes
+
+    import torch
+
+    from seismicmesh_gb300 import _device as D
+    from seismicmesh_gb300 import _native as N
+    from seismicmesh_gb300.generation.mesh_generator import _Engine
+
+    L = N.lib()
+    f = L.dmdbg_face_query_mode
+    f.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t,
+                  ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
+    eng = _Engine(3, P, 0)
+    eng.triangulate()  # builds the grid in the workspace
+    Fd = torch.from_numpy(np.ascontiguousarray(faces, dtype=np.int32)).to(D.device())
+    out = torch.empty(len(faces), dtype=torch.int32, device=D.device())
+    assert f(3, eng.P.data_ptr(), eng.n, eng.ws_dt.data_ptr(), eng.ws_dt.numel(), Fd.data_ptr(),
+             len(faces), out.data_ptr(), None, mode) == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), eng
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["lattice", "near_lattice", "rounded_lattice"])
+def test_face_queries_match_exhaustive_half_space_scan(cuda, kind):
+    """Region-bounded gift-wrap queries return the same point as a scan of
+    the whole positive half-space, on faces of (near-)degenerate lattices
+    where needle faces and huge circumspheres occur."""
+    rng = np.random.default_rng(5)
+    g = np.arange(-1.0, 1.0 + 1e-9, 0.1)
+    X = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    X[:, 0] += 0.05 * (np.round(X[:, 1] / 0.1) % 2)  # staggered rows
+    X = X[np.linalg.norm(X, axis=1) < 1.0]
+    if kind == "near_lattice":
+        X = X + 1e-6 * rng.standard_normal(X.shape)
+    elif kind == "rounded_lattice":
+        X = X * (1 + 1e-7 * rng.standard_normal(len(X)))[:, None]
+    P = X.astype(np.float32).astype(np.float64)
+    eng_cells = None
+    from seismicmesh_gb300.generation.mesh_generator import _Engine
+
+    e = _Engine(3, P, 0)
+    nc = e.triangulate()
+    eng_cells = e.cells[:nc].cpu().numpy()
+    sel = eng_cells[rng.choice(len(eng_cells), min(len(eng_cells), 3000), replace=False)]
+    faces = []
+    for c in sel:
+        for i in range(4):
+            o = [c[j] for j in range(4) if j != i]
+            for (u, v) in ((o[0], o[1]), (o[1], o[2]), (o[2], o[0]), (o[1], o[0]), (o[2], o[1]), (o[0], o[2])):
+                faces.append((c[i], u, v))
+    faces = np.array(faces)
+    got, _ = _face_queries(P, faces, 0)
+    want, _ = _face_queries(P, faces, 1)
+    bad = np.nonzero(got != want)[0]
+    assert len(bad) == 0, (len(bad), faces[bad[:5]].tolist(), got[bad[:5]].tolist(), want[bad[:5]].tolist())

@@ -198,3 +198,35 @@ def test_ball_against_oracle_end_metrics(cuda):
     ps, ts = sm.sliver_removal(p, sm.Ball([0.0, 0.0, 0.0], 1.0), 0.1, verbose=0)
     dhs = np.degrees(O.dihedral_angles(ps, ts)).reshape(-1, 6).min(1)
     assert dhs.min() >= 10.0 - 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3])
+def test_max_movement_is_written_where_it_is_read(cuda, dim):
+    """dm_update_points writes the maximum of |F| to maxf[dm_bar_blocks(n)]
+    in 2D and 3D, so the value read back never comes from stale memory."""
+    import torch
+
+    from seismicmesh_gb300.generation import mesh_generator as MG
+
+    rng = np.random.default_rng(3)
+    h = 0.05
+    p = rng.uniform(-0.7, 0.7, (3000, dim))
+    dom = sm.Disk([0.0, 0.0], 1.0) if dim == 2 else sm.Ball([0.0, 0.0, 0.0], 1.0)
+    fd = MG._Domain(dom)
+    sizing = MG._Sizing(h, dim)
+    eng = MG._Engine(dim, p, 0)
+    eng.triangulate()
+    eng.filter(fd, 0.1 * h)
+    eng.build_adjacency()
+    eng.maxf.fill_(1e30)
+    before = eng.P[:, :dim].cpu().numpy().astype(np.float64)
+    eng.step(sizing, [fd], 1 + 0.4 / 2 ** (dim - 1), 0.3, h, float(np.sqrt(np.finfo(float).eps) * h))
+    m = eng.max_movement(0.3)
+    after = eng.P[:, :dim].cpu().numpy().astype(np.float64)
+    torch.cuda.synchronize()
+    # points well inside the domain are not projected: they move by dt |F|
+    inner = (np.linalg.norm(before, axis=1) < 0.9) & (np.linalg.norm(after, axis=1) < 0.9)
+    disp = np.linalg.norm(after - before, axis=1)[inner].max()
+    assert np.isfinite(m) and m < 1e3, m
+    assert m >= disp * (1 - 1e-5), (m, disp)
