@@ -231,7 +231,7 @@ def run_ours(args, world, rank, local):
                D.ptr(eng.deg), sizing.struct, D.ptr(eng.partials), stream)
         N.call("dm_update_points", 3, D.ptr(eng.P), D.ptr(eng.P2), eng.n, D.ptr(eng.adj),
                eng.adj_cap, D.ptr(eng.deg), sizing.struct, D.ptr(eng.partials), L0mult, 0.30,
-               0, lv, 1, H, deps, D.ptr(eng.maxf), stream)
+               0, lv, 1, H, deps, D.ptr(eng.maxf), eng.grid_exp, stream)
         eng.P, eng.P2 = eng.P2, eng.P
 
     # warm-up: the checked path (duplicates / capacity handled)

@@ -44,6 +44,10 @@ extern "C" {
 #define DM_CNT_AUX 7
 #define DM_NCOUNTERS 16
 
+/* grid_exp value that disables position rounding (dm_update_points,
+ * dm_sliver_perturb) */
+#define DM_NO_GRID (-1000)
+
 #define DM_FLAG_CELL_OVERFLOW 1   /* cells capacity exceeded               */
 #define DM_FLAG_STAR_OVERFLOW 2   /* a vertex star exceeded its capacity   */
 #define DM_FLAG_SEED_FAILED 4     /* no Delaunay seed found for a vertex   */
@@ -183,7 +187,11 @@ int dm_unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
  *                    (level 0: points with d > 0; level k > 0: points with
  *                    0 < d < hmin / 1.5).  Writes points_out, per-block
  *                    maxima of |F| into the leading entries of maxf and
- *                    their maximum into maxf[nblk].
+ *                    their maximum into maxf[nblk].  With grid_exp >= -200
+ *                    the new positions are rounded to multiples of
+ *                    2^grid_exp (DM_NO_GRID disables the rounding); points
+ *                    on one such grid let dm_delaunay decide every
+ *                    predicate in fixed-point integer arithmetic.
  * dm_bar_blocks gives nblk for n points (the same for 2D and 3D); partials
  * is a workspace of 2*nblk + 3 doubles written by dm_bar_sums and read by
  * dm_update_points. */
@@ -197,7 +205,7 @@ int dm_update_points(int32_t dim, const float *points, float *points_out,
                      const double *partials, float L0mult, float delta_t,
                      int64_t nfix, const dm_sdf_program *levels,
                      int32_t n_levels, float hmin, float deps, float *maxf,
-                     void *stream);
+                     int32_t grid_exp, void *stream);
 /* bar midpoints per adjacency slot (float[n][adj_cap][dim]) for sizing
  * functions that are host callables */
 int dm_slot_midpoints(int32_t dim, const float *points, int64_t n,
@@ -239,12 +247,14 @@ int dm_dihedral_flags(const float *points, const int32_t *cells,
 /* perturb vertex 0 of each flagged cell by step*h0*normalize(grad R^2),
  * all perturbations computed from the pre-update positions; when a vertex is
  * vertex 0 of several flagged cells the highest cell index wins (numpy's
- * buffered fancy-index += keeps the last duplicate). */
+ * buffered fancy-index += keeps the last duplicate).  New positions are
+ * rounded to multiples of 2^grid_exp as in dm_update_points. */
 int dm_sliver_workspace_size(int64_t n_points, size_t *bytes);
 int dm_sliver_perturb(float *points, int64_t n_points, const int32_t *cells,
                       int64_t cap_cells, int32_t count_index,
-                      const int32_t *flags, float step_h0, void *workspace,
-                      size_t workspace_bytes, int64_t *counters, void *stream);
+                      const int32_t *flags, float step_h0, int32_t grid_exp,
+                      void *workspace, size_t workspace_bytes,
+                      int64_t *counters, void *stream);
 
 /* ---- gradient limiting -----------------------------------------------------
  * Replaces _FastHJ.limgrad (sizing/cpp/FastHJ.cpp:63-157): limits

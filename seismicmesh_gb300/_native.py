@@ -26,6 +26,7 @@ DM_ERR_CAPACITY = 3
 DM_ERR_NOT_CONVERGED = 4
 DM_ERR_DEGENERATE = 5
 DM_ERR_WORKSPACE = 6
+DM_NO_GRID = -1000
 
 CNT_CELLS, CNT_ESCALATED, CNT_FLAGS, CNT_KEPT, CNT_EDGES, CNT_BAD, CNT_DUPS, CNT_AUX = range(8)
 NCOUNTERS = 16
@@ -88,7 +89,7 @@ SIGNATURES = {
         c_int,
         [
             c_int, c_p, c_p, c_i64, c_p, c_int, c_p, ctypes.POINTER(Sizing), c_p,
-            c_f, c_f, c_i64, ctypes.POINTER(SdfProgram), c_int, c_f, c_f, c_p, c_p,
+            c_f, c_f, c_i64, ctypes.POINTER(SdfProgram), c_int, c_f, c_f, c_p, c_int, c_p,
         ],
     ),
     "dm_slot_midpoints": (c_int, [c_int, c_p, c_i64, c_p, c_int, c_p, c_p, c_p]),
@@ -99,7 +100,7 @@ SIGNATURES = {
     "dm_circumsphere_grad": (c_int, [c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "dm_dihedral_flags": (c_int, [c_p, c_p, c_i64, c_int, c_f, c_f, c_p, c_p, c_p]),
     "dm_sliver_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
-    "dm_sliver_perturb": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_p, c_f, c_p, c_sz, c_p, c_p]),
+    "dm_sliver_perturb": (c_int, [c_p, c_i64, c_p, c_i64, c_int, c_p, c_f, c_int, c_p, c_sz, c_p, c_p]),
     "dm_limgrad": (c_int, [ctypes.POINTER(c_int), c_d, c_d, c_int, c_p, c_p]),
     "dm_boundary_workspace_size": (c_int, [c_int, c_i64, c_i64, ctypes.POINTER(c_sz)]),
     "dm_boundary": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_p, c_i64, c_p, c_p, c_sz, c_p]),

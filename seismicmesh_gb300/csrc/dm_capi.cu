@@ -25,7 +25,7 @@ int update_points(int dim, const float *P, float *Pout, int64_t n,
                   const dm_sizing *sz, const double *partials, float L0mult,
                   float dt, int64_t nfix, const dm_sdf_program *levels,
                   int n_levels, float hmin, float deps, float *maxf,
-                  cudaStream_t s);
+                  int grid_exp, cudaStream_t s);
 int slot_midpoints(int dim, const float *P, int64_t n, const int32_t *adj,
                    int adj_cap, const int32_t *deg, float *mid, cudaStream_t s);
 int sdf_eval_launch(const dm_sdf_program *p, const float *x, int64_t n,
@@ -43,8 +43,8 @@ int dihedral_flags(const float *P, const int32_t *cells, int64_t cap,
                    int64_t *counters, cudaStream_t s);
 int sliver_perturb(float *P, int64_t n_points, const int32_t *cells,
                    int64_t cap, int count_index, const int32_t *flags,
-                   float step_h0, void *ws, size_t ws_bytes, int64_t *counters,
-                   cudaStream_t s);
+                   float step_h0, int grid_exp, void *ws, size_t ws_bytes,
+                   int64_t *counters, cudaStream_t s);
 size_t sliver_workspace(int64_t n_points);
 int limgrad(const int32_t *dims, double elen, double dfdx, int imax, double *f,
             cudaStream_t s);
@@ -187,10 +187,10 @@ int dm_update_points(int32_t dim, const float *points, float *points_out,
                      const double *partials, float L0mult, float delta_t,
                      int64_t nfix, const dm_sdf_program *levels,
                      int32_t n_levels, float hmin, float deps, float *maxf,
-                     void *stream) {
+                     int32_t grid_exp, void *stream) {
   return dm::update_points(dim, points, points_out, n, adj, adj_cap, deg,
                            sizing, partials, L0mult, delta_t, nfix, levels,
-                           n_levels, hmin, deps, maxf, S(stream));
+                           n_levels, hmin, deps, maxf, grid_exp, S(stream));
 }
 int dm_slot_midpoints(int32_t dim, const float *points, int64_t n,
                       const int32_t *adj, int32_t adj_cap, const int32_t *deg,
@@ -235,11 +235,12 @@ int dm_sliver_workspace_size(int64_t n_points, size_t *bytes) {
 }
 int dm_sliver_perturb(float *points, int64_t n_points, const int32_t *cells,
                       int64_t cap_cells, int32_t count_index,
-                      const int32_t *flags, float step_h0, void *workspace,
-                      size_t workspace_bytes, int64_t *counters, void *stream) {
+                      const int32_t *flags, float step_h0, int32_t grid_exp,
+                      void *workspace, size_t workspace_bytes,
+                      int64_t *counters, void *stream) {
   return dm::sliver_perturb(points, n_points, cells, cap_cells, count_index,
-                            flags, step_h0, workspace, workspace_bytes,
-                            counters, S(stream));
+                            flags, step_h0, grid_exp, workspace,
+                            workspace_bytes, counters, S(stream));
 }
 
 int dm_limgrad(const int32_t *dims, double elen, double dfdx, int32_t imax,

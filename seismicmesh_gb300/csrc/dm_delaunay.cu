@@ -24,6 +24,7 @@
 // whose queries walk the uniform grid and its coarse blocks and are exact
 // over the whole point set.
 #include <float.h>
+#include <limits.h>
 #include <string.h>
 
 #include "dm_common.cuh"
@@ -44,7 +45,12 @@ struct GridParams {
   int bdims[3];
   int nblocks;
   int dim;
+  // every coordinate is a multiple of 2^gfix and |coordinate| < 2^(gfix+29):
+  // all predicates can use the fixed-point path; kNoFix otherwise
+  int gfix;
 };
+
+constexpr int kNoFix = -100000;
 
 struct DTArgs {
   int dim;
@@ -114,12 +120,23 @@ __global__ void k_bbox_init(int *bbox) {
     bbox[threadIdx.x] = f2o(FLT_MAX);
     bbox[3 + threadIdx.x] = f2o(-FLT_MAX);
   }
+  if (threadIdx.x == 0) bbox[6] = INT_MAX;  // smallest lowest-set-bit exponent
+}
+
+// exponent of the lowest set bit of a finite non-zero float; INT_MAX for 0
+__device__ __forceinline__ int lsb_exponent(float x) {
+  uint32_t u = __float_as_uint(x);
+  int e = (int)((u >> 23) & 0xffu);
+  uint32_t m = u & 0x7fffffu;
+  if (e == 0) return m ? -149 + __ffs(m) - 1 : INT_MAX;
+  return e - 150 + __ffs(m | 0x800000u) - 1;
 }
 
 template <int DIM>
 __global__ void k_bbox(const float *P, int64_t n, int *bbox, int64_t *counters) {
   float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
   bool bad = false;
+  int lsb = INT_MAX;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float x[3];
@@ -128,8 +145,11 @@ __global__ void k_bbox(const float *P, int64_t n, int *bbox, int64_t *counters) 
       if (!isfinite(x[k])) bad = true;
       mn[k] = fminf(mn[k], x[k]);
       mx[k] = fmaxf(mx[k], x[k]);
+      lsb = min(lsb, lsb_exponent(x[k]));
     }
   }
+  for (int o = 16; o; o >>= 1) lsb = min(lsb, __shfl_xor_sync(0xffffffffu, lsb, o));
+  if ((threadIdx.x & 31) == 0 && lsb != INT_MAX) atomicMin(&bbox[6], lsb);
   for (int k = 0; k < DIM; ++k) {
     for (int o = 16; o; o >>= 1) {
       mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
@@ -188,6 +208,14 @@ __global__ void k_grid_params(GridParams *gp, const int *bbox, int64_t n,
   // round cs up to a float that keeps floor((x-lo)/cs) within dims
   GridParams g;
   g.dim = dim;
+  // common power-of-two grid of the coordinates (fixed-point predicates)
+  g.gfix = kNoFix;
+  if (finite) {
+    double E = 0;
+    for (int k = 0; k < dim; ++k) E = fmax(E, fmax(fabs(lo[k]), fabs(lo[k] + ext[k])));
+    int lsb = bbox[6];
+    if (E > 0 && lsb != INT_MAX && lsb >= ilogb(E) - 28) g.gfix = lsb;
+  }
   g.cs = (float)cs;
   g.inv_cs = (float)(1.0 / cs);
   g.ncells = 1;
@@ -503,10 +531,17 @@ struct FxFrame {
   long long P0[3];
 };
 
+// gfix != kNoFix: every point shares the grid 2^gfix (range checked when the
+// grid was built), so that scale serves every star
 template <int DIM>
-__device__ __forceinline__ void fx_frame(FxFrame &fr, const float *p, float extent) {
-  fr.g = dmp::float_exponent(extent) - 28;
-  fr.ok = extent > 0.f && dmp::float_exponent(extent) > -100;
+__device__ __forceinline__ void fx_frame(FxFrame &fr, const float *p, float extent, int gfix) {
+  if (gfix != kNoFix) {
+    fr.g = gfix;
+    fr.ok = true;
+  } else {
+    fr.g = dmp::float_exponent(extent) - 28;
+    fr.ok = extent > 0.f && dmp::float_exponent(extent) > -100;
+  }
   for (int k = 0; k < 3; ++k) fr.P0[k] = 0;
   for (int k = 0; k < DIM; ++k) fr.ok = fr.ok && dmp::float_to_fixed(p[k], fr.g, &fr.P0[k]);
 }
@@ -531,7 +566,7 @@ __device__ __forceinline__ int4 fx_point(const FxFrame &fr, const float *x) {
 // representation keeps w = 0 and uses the floating-point exact path.
 template <int DIM>
 __device__ __forceinline__ void fixed_coords(WarpL1<DIM> &S, const DTArgs &A,
-                                             const float *px, int lane) {
+                                             const float *px, int lane, int gfix) {
   const int nc = S.nc;
   float m = 0.f;
   for (int j = lane; j < nc; j += 32) {
@@ -540,7 +575,7 @@ __device__ __forceinline__ void fixed_coords(WarpL1<DIM> &S, const DTArgs &A,
   }
   for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   FxFrame fr;
-  fx_frame<DIM>(fr, px, m);
+  fx_frame<DIM>(fr, px, m, gfix);
   for (int j = lane; j < nc; j += 32) {
     float xq[3];
     load_pt<DIM>(A.P, S.id[j], xq);
@@ -653,7 +688,7 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
   __syncwarp();
   if (lane == 0 && S.nc > L1<DIM>::CAP) S.nc = L1<DIM>::CAP;  // cannot happen
   __syncwarp();
-  fixed_coords<DIM>(S, A, px, lane);
+  fixed_coords<DIM>(S, A, px, lane, g.gfix);
 }
 
 // is the cell (p, a, b, c) of a packed link triangle empty w.r.t. every
@@ -1191,10 +1226,10 @@ struct Face3 {
   int4 IA, IB;   // a, b in that frame
 };
 
-__device__ __forceinline__ void face3_frame(Face3 &F) {
+__device__ __forceinline__ void face3_frame(Face3 &F, int gfix) {
   float e = 0.f;
   for (int k = 0; k < 3; ++k) e = fmaxf(e, fmaxf(fabsf(F.V[k]), fabsf(F.U[k])));
-  fx_frame<3>(F.fr, F.p, 8.f * e);
+  fx_frame<3>(F.fr, F.p, 8.f * e, gfix);
   F.IA = fx_point<3>(F.fr, F.a);
   F.IB = fx_point<3>(F.fr, F.b);
 }
@@ -1302,6 +1337,8 @@ struct Region3 {
   double cc[3], r2, Z, dcc;  // kind 1 (cc absolute), dcc: error bound of cc
   double s[3], R2;           // kind 2
   double lo[3], hi[3];       // bounding box of the region (kinds 1, 2)
+  // FP32 copies for the per-box tests (FP64 stays out of the scan loops)
+  float fp[3], fun[3], fc[3], fr2, fZ, fR2, fdcc;
 };
 
 // double-precision region from the exact face/winner differences
@@ -1326,7 +1363,7 @@ __device__ __forceinline__ void make_region3(Region3 &R, const float *fp, const 
                     (t[0] * n[1] - t[1] * n[0]) * inv};
     double r2 = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2];
     double r = sqrt(r2);
-    double dcc = 16 * u * (la * bl + lb * al) * al * bl / nn + 1e-9 * r;
+    double dcc = 16 * u * (la * bl + lb * al) * al * bl / nn + 4 * u * r;
     double w[3] = {c[0] - cc[0], c[1] - cc[1], c[2] - cc[2]};
     double lw = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
     double q = lw - r2;
@@ -1394,42 +1431,51 @@ __device__ __forceinline__ void make_region3(Region3 &R, const float *fp, const 
   }
 }
 
-// may the box [lo, hi] hold a point of the region?  (conservative)
+__device__ __forceinline__ void region3_floats(Region3 &R) {
+  for (int k = 0; k < 3; ++k) {
+    R.fp[k] = (float)R.p[k];
+    R.fun[k] = (float)R.un[k];
+    R.fc[k] = (float)(R.kind == 2 ? R.s[k] : R.cc[k]);
+  }
+  R.fr2 = (float)R.r2;
+  R.fZ = (float)fmax(fmin(R.Z, 1e30), -1e30);
+  R.fR2 = (float)fmin(R.R2, 1e36);
+  R.fdcc = (float)R.dcc;
+}
+
+// May the box [lo, hi] hold a point of the region?  Conservative FP32 test:
+// every rounding error (a few ulps per term, relative 6e-8) is covered by
+// margins of relative 1e-5 and by the error bound of the region itself.
 __device__ __forceinline__ bool region_hits3(const Region3 &R, const float *lo,
                                              const float *hi) {
-  // heights of the box corners over the face plane, and distance bounds
-  double zmin = 1e300, zmax = -1e300, dp2 = 0;
+  // heights of the box corners over the face plane, distance bound to p
+  float zmin = FLT_MAX, zmax = -FLT_MAX, dp2 = 0.f;
   for (int corner = 0; corner < 8; ++corner) {
-    double z = 0, d2 = 0;
+    float z = 0.f, d2 = 0.f;
     for (int k = 0; k < 3; ++k) {
-      double v = (double)((corner >> k) & 1 ? hi[k] : lo[k]) - R.p[k];
-      z += v * R.un[k];
-      d2 += v * v;
+      float v = ((corner >> k) & 1 ? hi[k] : lo[k]) - R.fp[k];
+      z = fmaf(v, R.fun[k], z);
+      d2 = fmaf(v, v, d2);
     }
-    zmin = fmin(zmin, z);
-    zmax = fmax(zmax, z);
-    dp2 = fmax(dp2, d2);
+    zmin = fminf(zmin, z);
+    zmax = fmaxf(zmax, z);
+    dp2 = fmaxf(dp2, d2);
   }
-  const double dp = sqrt(dp2);
-  if (R.cull && zmax < -1e-5 * dp) return false;  // entirely below the face
+  const float dp = sqrtf(dp2);
+  const float tz = 1e-5f * dp;  // height error (normal direction and rounding)
+  if (R.cull && zmax < -tz) return false;  // entirely below the face
   if (R.kind == 0) return true;
-  if (R.kind == 2) {
-    double d2 = 0;
-    for (int k = 0; k < 3; ++k) {
-      double e = fmax(fmax((double)lo[k] - R.s[k], R.s[k] - (double)hi[k]), 0.0);
-      d2 += e * e;
-    }
-    return d2 <= R.R2 * (1 + 1e-9) + 1e-30;
-  }
-  // kind 1: lower bound of |x-cc|^2 - 2 Z z(x) - r^2 over the box within H+
-  double d2 = 0;
+  float d2 = 0.f;
   for (int k = 0; k < 3; ++k) {
-    double e = fmax(fmax((double)lo[k] - R.cc[k], R.cc[k] - (double)hi[k]), 0.0);
-    d2 += e * e;
+    float e = fmaxf(fmaxf(lo[k] - R.fc[k], R.fc[k] - hi[k]), 0.f);
+    d2 = fmaf(e, e, d2);
   }
-  double zb = R.Z > 0 ? zmax : fmax(zmin, 0.0);
-  double gl = d2 - 2 * R.Z * zb - R.r2;
-  double tol = 2 * dp * R.dcc + 1e-9 * (d2 + R.r2 + fabs(2 * R.Z * zb)) + 1e-8 * dp * fabs(2 * R.Z);
+  if (R.kind == 2) return d2 <= R.fR2 * (1.f + 1e-5f) + 1e-30f;
+  // kind 1: lower bound of |x-cc|^2 - 2 Z z(x) - r^2 over the box within H+
+  float zb = R.fZ > 0.f ? zmax + tz : fmaxf(zmin - tz, 0.f);
+  float t = 2.f * R.fZ * zb;
+  float gl = d2 - t - R.fr2;
+  float tol = 2.f * dp * R.fdcc + 1e-5f * (d2 + R.fr2 + fabsf(t)) + 1e-30f;
   return gl <= tol;
 }
 
@@ -1453,7 +1499,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     F.V[k] = F.a[k] - F.p[k];
     F.U[k] = F.b[k] - F.p[k];
   }
-  face3_frame(F);
+  face3_frame(F, g.gfix);
   // face normal from the exact differences
   double a[3], b[3];
   for (int k = 0; k < 3; ++k) {
@@ -1480,8 +1526,16 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   // after a tournament every lane holds the same winner: reload its point
   best = tourney3(A, F, best, ovf, W);
   if (best >= 0) load_pt<3>(A.P, best, bx);
+#ifdef DM_L2_STATS
+  const long long tr_t0 = clock64();
+  const int tr_local = best;
+  int tr_wide = -2;
+  const int tr_w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const unsigned long long tr_c0 = tr_w < kL2StatWarps ? g_l2w[tr_w][3] : 0;
+#endif
   Region3 R;
   make_region3(R, F.p, a, b, n, nn, la, lb, best >= 0 ? bx : nullptr);
+  region3_floats(R);
   int rex = 1;  // cells with Chebyshev distance <= rex are done
   // a large region: widen the local search to the 5^3 cells first
   bool large = R.kind == 0;
@@ -1496,6 +1550,10 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     rex = 2;
     if (best >= 0) load_pt<3>(A.P, best, bx);
     make_region3(R, F.p, a, b, n, nn, la, lb, best >= 0 ? bx : nullptr);
+    region3_floats(R);
+#ifdef DM_L2_STATS
+    tr_wide = best;
+#endif
   }
   if (A.dbg_full) {
     R.kind = 0;
@@ -1567,7 +1625,35 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
           }
     }
   }
-  return tourney3(A, F, best, ovf, W);
+  best = tourney3(A, F, best, ovf, W);
+#ifdef DM_L2_STATS
+  // per-face trace of the watched vertex: dbg[1999] counts faces, record
+  // i at dbg[2000 + 16 i]
+  if (ip == A.dbg_vertex && A.dbg && lane == 0) {
+    int i = atomicAdd(&A.dbg[1999], 1);
+    if (i < 256) {
+      int32_t *t = A.dbg + 2000 + 16 * i;
+      int64_t ncell = 1;
+      for (int k = 0; k < 3; ++k) ncell *= max(1, (int)((R.hi[k] - R.lo[k]) * g.inv_cs) + 1);
+      t[0] = ia;
+      t[1] = ib;
+      t[2] = R.kind;
+      t[3] = (int)min(ncell, (int64_t)INT32_MAX);
+      t[4] = tr_local;
+      t[5] = tr_wide;
+      t[6] = best;
+      t[7] = (int)min(clock64() - tr_t0, (long long)INT32_MAX);
+      t[8] = tr_w < kL2StatWarps ? (int)(g_l2w[tr_w][3] - tr_c0) : -1;
+      t[9] = __float_as_int((float)R.Z);
+      t[10] = __float_as_int((float)R.r2);
+      t[11] = __float_as_int((float)R.R2);
+      t[12] = rex;
+      t[13] = F.IA.w | (F.IB.w << 1) | ((int)F.fr.ok << 2);
+      t[14] = F.fr.g;
+    }
+  }
+#endif
+  return best;
 }
 
 // ---- 2D exhaustive query across edge (p, x): sgn=+1 triangles (p,x,y),
@@ -1580,8 +1666,8 @@ struct Edge2 {
   int4 IX;
 };
 
-__device__ __forceinline__ void edge2_frame(Edge2 &E) {
-  fx_frame<2>(E.fr, E.p, 8.f * fmaxf(fabsf(E.X[0]), fabsf(E.X[1])));
+__device__ __forceinline__ void edge2_frame(Edge2 &E, int gfix) {
+  fx_frame<2>(E.fr, E.p, 8.f * fmaxf(fabsf(E.X[0]), fabsf(E.X[1])), gfix);
   E.IX = fx_point<2>(E.fr, E.x);
 }
 
@@ -1664,7 +1750,7 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
   load_pt<2>(A.P, ix, E.x);
   E.X[0] = E.x[0] - E.p[0];
   E.X[1] = E.x[1] - E.p[1];
-  edge2_frame(E);
+  edge2_frame(E, g.gfix);
   int best = -1;
   float bx[2];
   int cc[3] = {cell_coord(g, 0.5f * (E.p[0] + E.x[0]), 0),

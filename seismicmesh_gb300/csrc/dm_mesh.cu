@@ -301,12 +301,19 @@ __device__ __forceinline__ void newton_project(const Levels &L, float *x,
   }
 }
 
+// round x to a multiple of 2^e (exact: power-of-two scaling and rint);
+// e < -200 leaves x unchanged
+__device__ __forceinline__ float to_grid(float x, int e) {
+  return e < -200 ? x : ldexpf(rintf(ldexpf(x, -e)), e);
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(256)
     k_update(const float *P, float *Pout, int64_t n, const int32_t *adj,
              int adj_cap, const int32_t *deg, SizingDev sz,
              const double *partials, int nblk, float L0mult, float dt,
-             int64_t nfix, Levels lv, float hmin, float deps, float *maxf) {
+             int64_t nfix, Levels lv, float hmin, float deps, float *maxf,
+             int grid_exp) {
   constexpr int G = BarCfg<DIM>::G;
   const int sub = threadIdx.x % G;
   int64_t v = (int64_t)blockIdx.x * BarCfg<DIM>::VPB + threadIdx.x / G;
@@ -345,6 +352,7 @@ __global__ void __launch_bounds__(256)
       fn += F[j] * F[j];
     }
     newton_project<DIM>(lv, x, hmin, deps);
+    for (int j = 0; j < DIM; ++j) x[j] = to_grid(x[j], grid_exp);
     if (DIM == 3)
       reinterpret_cast<float4 *>(Pout)[v] = make_float4(x[0], x[1], x[2], 0.f);
     else
@@ -608,13 +616,14 @@ __global__ void k_sliver_delta(const float *P, const int32_t *cells, int64_t cap
 }
 
 __global__ void k_sliver_apply(float *P, int64_t n, const int32_t *winner,
-                               const float4 *delta) {
+                               const float4 *delta, int grid_exp) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     if (winner[v] < 0) continue;
     float4 p = reinterpret_cast<float4 *>(P)[v], d = delta[v];
     reinterpret_cast<float4 *>(P)[v] =
-        make_float4(p.x + d.x, p.y + d.y, p.z + d.z, 0.f);
+        make_float4(to_grid(p.x + d.x, grid_exp), to_grid(p.y + d.y, grid_exp),
+                    to_grid(p.z + d.z, grid_exp), 0.f);
   }
 }
 
@@ -707,7 +716,7 @@ int update_points(int dim, const float *P, float *Pout, int64_t n,
                   const dm_sizing *sz, const double *partials, float L0mult,
                   float dt, int64_t nfix, const dm_sdf_program *levels,
                   int n_levels, float hmin, float deps, float *maxf,
-                  cudaStream_t s) {
+                  int grid_exp, cudaStream_t s) {
   DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
   DM_ARG_CHECK(n_levels >= 0 && n_levels <= 4, "at most 4 levels");
   Levels L;
@@ -720,10 +729,12 @@ int update_points(int dim, const float *P, float *Pout, int64_t n,
   SizingDev d = to_dev(sz);
   if (dim == 3)
     k_update<3><<<nblk, 256, 0, s>>>(P, Pout, n, adj, adj_cap, deg, d, partials,
-                                     nblk, L0mult, dt, nfix, L, hmin, deps, maxf);
+                                     nblk, L0mult, dt, nfix, L, hmin, deps, maxf,
+                                     grid_exp);
   else
     k_update<2><<<nblk, 256, 0, s>>>(P, Pout, n, adj, adj_cap, deg, d, partials,
-                                     nblk, L0mult, dt, nfix, L, hmin, deps, maxf);
+                                     nblk, L0mult, dt, nfix, L, hmin, deps, maxf,
+                                     grid_exp);
   // the result goes to maxf[dm_bar_blocks(n)], the slot callers size
   // (and read) independently of the dimension
   const int slot = max(bar_blocks(2, n), bar_blocks(3, n));
@@ -809,8 +820,8 @@ int dihedral_flags(const float *P, const int32_t *cells, int64_t cap,
 
 int sliver_perturb(float *P, int64_t n_points, const int32_t *cells,
                    int64_t cap, int count_index, const int32_t *flags,
-                   float step_h0, void *ws, size_t ws_bytes, int64_t *counters,
-                   cudaStream_t s) {
+                   float step_h0, int grid_exp, void *ws, size_t ws_bytes,
+                   int64_t *counters, cudaStream_t s) {
   Carve c(ws, ws_bytes);
   int32_t *winner = c.take<int32_t>(n_points);
   float4 *delta = c.take<float4>(n_points);
@@ -823,7 +834,8 @@ int sliver_perturb(float *P, int64_t n_points, const int32_t *cells,
   k_sliver_winner<<<nb, 256, 0, s>>>(cells, cap, count_index, flags, counters, winner);
   k_sliver_delta<<<nb, 256, 0, s>>>(P, cells, cap, count_index, flags, counters,
                                     winner, step_h0, delta);
-  k_sliver_apply<<<grid_for(n_points, 256), 256, 0, s>>>(P, n_points, winner, delta);
+  k_sliver_apply<<<grid_for(n_points, 256), 256, 0, s>>>(P, n_points, winner, delta,
+                                                          grid_exp);
   DM_LAUNCH_CHECK();
   return DM_OK;
 }

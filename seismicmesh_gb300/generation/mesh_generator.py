@@ -117,12 +117,38 @@ class _Sizing:
 
 
 # ---------------------------------------------------------------------------
-class _Engine:
-    """Device state of one meshing run."""
+def position_grid_exponent(p):
+    """Exponent e of the position grid 2^e of a run: 24 bits below the
+    largest coordinate magnitude (with 25% headroom), i.e. the resolution a
+    float32 has at that magnitude.  Points on one such grid let the Delaunay
+    kernels decide every predicate in fixed-point integer arithmetic."""
+    p = np.asarray(p, dtype=float)
+    E = float(np.abs(p).max()) * 1.25 if p.size else 1.0
+    if not np.isfinite(E) or E <= 0:
+        return N.DM_NO_GRID
+    return math.frexp(E)[1] - 1 - 24
 
-    def __init__(self, dim, p_host, nfix):
+
+def snap_to_grid(p, e):
+    """p rounded to multiples of 2^e (float64, exactly representable in float32)."""
+    if e == N.DM_NO_GRID:
+        return np.asarray(p, dtype=float)
+    q = math.ldexp(1.0, e)
+    return np.rint(np.asarray(p, dtype=float) / q) * q
+
+
+class _Engine:
+    """Device state of one meshing run.  With grid=True the points live on the
+    position grid of the run (snapped here, kept there by the update
+    kernels); grid=False keeps the caller's float32 points unchanged."""
+
+    def __init__(self, dim, p_host, nfix, grid=True):
         self.dim = dim
         self.nfix = nfix
+        p_host = np.asarray(p_host, dtype=float)
+        self.grid_exp = position_grid_exponent(p_host) if grid else N.DM_NO_GRID
+        if grid:
+            p_host = snap_to_grid(p_host, self.grid_exp)
         self.set_points(D.to_points(p_host, dim))
         self.counters = D.zeros((N.NCOUNTERS,), torch.int64)
         self.adj_cap = ADJ_CAP[dim]
@@ -244,7 +270,7 @@ class _Engine:
             "dm_update_points", self.dim, D.ptr(self.P), D.ptr(self.P2), self.n,
             D.ptr(self.adj), self.adj_cap, D.ptr(self.deg), sizing.struct,
             D.ptr(self.partials), L0mult, delta_t, self.nfix, lv, len(levels), h0,
-            deps, D.ptr(self.maxf), D.stream_ptr(),
+            deps, D.ptr(self.maxf), self.grid_exp, D.stream_ptr(),
         )
         self.P, self.P2 = self.P2, self.P
 
@@ -565,8 +591,8 @@ def sliver_removal(points, domain, edge_length, comm=None, **kwargs):  # noqa: C
         w = D.workspace(ws.value)
         N.call(
             "dm_sliver_perturb", D.ptr(eng.P), eng.n, D.ptr(eng.kept), eng.cap_cells,
-            N.CNT_KEPT, D.ptr(flags), step * h0, D.ptr(w), w.numel(), D.ptr(eng.counters),
-            D.stream_ptr(),
+            N.CNT_KEPT, D.ptr(flags), step * h0, eng.grid_exp, D.ptr(w), w.numel(),
+            D.ptr(eng.counters), D.stream_ptr(),
         )
         if sliver_opts["preserve"]:
             eng.improve_level_set(fd, deps)

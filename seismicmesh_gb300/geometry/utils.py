@@ -160,7 +160,7 @@ def laplacian2_fixed_point(vertices, entities):
     vertices = np.asarray(vertices)
     if vertices.ndim != 2 or vertices.shape[1] != 2:
         raise NotImplementedError("Laplacian smoothing only works in 2D for now")
-    eng = _Engine(2, vertices, 0)
+    eng = _Engine(2, vertices, 0, grid=False)
     t = np.ascontiguousarray(entities, dtype=np.int32)
     eng.kept[: len(t)] = torch.from_numpy(t).to(eng.P.device)
     eng.counters[N.CNT_KEPT] = len(t)
@@ -194,7 +194,7 @@ def delete_boundary_entities(vertices, entities, dim=2, min_qual=0.10, verbose=1
     """Delete boundary cells of quality < min_qual (geometry/utils.py:440-469)."""
     from ..generation.mesh_generator import _Engine
 
-    eng = _Engine(dim, np.asarray(vertices), 0)
+    eng = _Engine(dim, np.asarray(vertices), 0, grid=False)
     t = np.ascontiguousarray(entities, dtype=np.int32)
     eng.kept[: len(t)] = torch.from_numpy(t).to(eng.P.device)
     eng.counters[N.CNT_KEPT] = len(t)

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 
 def triangulate(p):
-    eng = _Engine(p.shape[1], p, 0)
+    eng = _Engine(p.shape[1], p, 0, grid=False)
     nc = eng.triangulate()
     return eng.cells[:nc].cpu().numpy(), eng.counters_host()
 
@@ -86,13 +86,13 @@ def test_duplicate_points_are_merged_like_cgal(cuda):
     rng = np.random.default_rng(3)
     p = rng.random((500, 3)).astype(np.float32).astype(np.float64)
     q = np.vstack([p, p[:20]])
-    eng = _Engine(3, q, 0)
+    eng = _Engine(3, q, 0, grid=False)
     nc = eng.triangulate()
     assert eng.n == 500
     dc.assert_same_triangulation(eng.P[:, :3].double().cpu().numpy(), eng.cells[:nc].cpu().numpy())
 
 
-def _face_queries(P, faces, mode):
+def _face_queries(P, faces, mode, grid=False):
     import ctypes
 
     import torch
@@ -105,7 +105,7 @@ def _face_queries(P, faces, mode):
     f = L.dmdbg_face_query_mode
     f.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_size_t,
                   ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
-    eng = _Engine(3, P, 0)
+    eng = _Engine(3, P, 0, grid=grid)
     eng.triangulate()  # builds the grid in the workspace
     Fd = torch.from_numpy(np.ascontiguousarray(faces, dtype=np.int32)).to(D.device())
     out = torch.empty(len(faces), dtype=torch.int32, device=D.device())
@@ -116,7 +116,7 @@ def _face_queries(P, faces, mode):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["lattice", "near_lattice", "rounded_lattice"])
+@pytest.mark.parametrize("kind", ["lattice", "near_lattice", "rounded_lattice", "grid_near_lattice"])
 def test_face_queries_match_exhaustive_half_space_scan(cuda, kind):
     """Region-bounded gift-wrap queries return the same point as a scan of
     the whole positive half-space, on faces of (near-)degenerate lattices
@@ -130,11 +130,17 @@ def test_face_queries_match_exhaustive_half_space_scan(cuda, kind):
         X = X + 1e-6 * rng.standard_normal(X.shape)
     elif kind == "rounded_lattice":
         X = X * (1 + 1e-7 * rng.standard_normal(len(X)))[:, None]
+    elif kind == "grid_near_lattice":
+        from seismicmesh_gb300.generation.mesh_generator import position_grid_exponent, snap_to_grid
+
+        X = X + 1e-6 * rng.standard_normal(X.shape)
+        X = snap_to_grid(X, position_grid_exponent(X))
+    grid = kind.startswith("grid")
     P = X.astype(np.float32).astype(np.float64)
     eng_cells = None
     from seismicmesh_gb300.generation.mesh_generator import _Engine
 
-    e = _Engine(3, P, 0)
+    e = _Engine(3, P, 0, grid=grid)
     nc = e.triangulate()
     eng_cells = e.cells[:nc].cpu().numpy()
     sel = eng_cells[rng.choice(len(eng_cells), min(len(eng_cells), 3000), replace=False)]
@@ -145,7 +151,23 @@ def test_face_queries_match_exhaustive_half_space_scan(cuda, kind):
             for (u, v) in ((o[0], o[1]), (o[1], o[2]), (o[2], o[0]), (o[1], o[0]), (o[2], o[1]), (o[0], o[2])):
                 faces.append((c[i], u, v))
     faces = np.array(faces)
-    got, _ = _face_queries(P, faces, 0)
-    want, _ = _face_queries(P, faces, 1)
+    got, _ = _face_queries(P, faces, 0, grid)
+    want, _ = _face_queries(P, faces, 1, grid)
     bad = np.nonzero(got != want)[0]
     assert len(bad) == 0, (len(bad), faces[bad[:5]].tolist(), got[bad[:5]].tolist(), want[bad[:5]].tolist())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,n", [(2, 20000), (3, 20000)])
+def test_grid_aligned_points_match_qhull(cuda, dim, n):
+    """Points on a common power-of-two grid (as DistMesh keeps them) take the
+    fixed-point path for every predicate; the triangulation is Qhull's."""
+    from seismicmesh_gb300.generation.mesh_generator import _Engine, position_grid_exponent, snap_to_grid
+
+    rng = np.random.default_rng(17 + dim)
+    p = rng.uniform(-1, 1, (n, dim))
+    p = snap_to_grid(p, position_grid_exponent(p))
+    eng = _Engine(dim, p, 0, grid=True)
+    assert np.array_equal(eng.P[:, :dim].cpu().numpy().astype(np.float64), p)
+    nc = eng.triangulate()
+    dc.assert_same_triangulation(p, eng.cells[:nc].cpu().numpy())

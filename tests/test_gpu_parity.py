@@ -24,7 +24,7 @@ RTOL = 1e-5
 
 def _one_iteration(p0, domain, h):
     dim = p0.shape[1]
-    eng = MG._Engine(dim, p0, 0)
+    eng = MG._Engine(dim, p0, 0, grid=False)
     eng.triangulate()
     fd = MG._Domain(domain)
     eng.filter(fd, 0.1 * h)
