@@ -139,11 +139,15 @@ int dm_cell_centroids(int32_t dim, const float *points, const int32_t *cells,
  * (int32[n][adj_cap], device) lists the neighbours of v in increasing order,
  * deg[v] their count.  Cells are read from `cells` with count
  * counters[count_index].  counters[DM_CNT_EDGES] receives the number of
- * unique edges. */
+ * unique edges.  A vertex with more than adj_cap neighbours keeps the
+ * adj_cap smallest and raises DM_FLAG_ADJ_OVERFLOW (call again with a larger
+ * adj_cap).  The workspace holds the raw per-vertex neighbour lists. */
+int dm_adjacency_workspace_size(int32_t dim, int64_t n, int64_t cap_cells,
+                                size_t *bytes);
 int dm_adjacency(int32_t dim, int64_t n, const int32_t *cells,
                  int64_t cap_cells, int32_t count_index, int32_t *adj,
                  int32_t adj_cap, int32_t *deg, int64_t *counters,
-                 void *stream);
+                 void *workspace, size_t workspace_bytes, void *stream);
 /* Drop-in unique_edges: edges int32[m][2] -> sorted unique (min,max) pairs.
  * Needs the vertex count bound n (max index + 1). */
 int dm_unique_edges_workspace_size(int64_t n, int64_t m, size_t *bytes);

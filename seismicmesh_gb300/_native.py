@@ -79,7 +79,8 @@ SIGNATURES = {
         [c_int, c_p, c_p, c_i64, ctypes.POINTER(SdfProgram), c_f, c_p, c_p, c_p, c_sz, c_p],
     ),
     "dm_cell_centroids": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
-    "dm_adjacency": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_int, c_p, c_p, c_p]),
+    "dm_adjacency_workspace_size": (c_int, [c_int, c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_adjacency": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_int, c_p, c_p, c_p, c_sz, c_p]),
     "dm_unique_edges_workspace_size": (c_int, [c_i64, c_i64, ctypes.POINTER(c_sz)]),
     "dm_unique_edges": (c_int, [c_p, c_i64, c_i64, c_p, ctypes.POINTER(c_i64), c_p, c_sz, c_p]),
     "dm_unique_edges_noalloc": (c_int, [c_p, c_i64, c_i64, c_p, ctypes.POINTER(c_i64), c_p]),

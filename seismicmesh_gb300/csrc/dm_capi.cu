@@ -13,9 +13,10 @@ int filter_cells(int dim, const float *P, const int32_t *cells, int64_t cap,
                  int64_t *counters, cudaStream_t s);
 int cell_centroids(int dim, const float *P, const int32_t *cells, int64_t cap,
                    const int64_t *counters, float *cen, cudaStream_t s);
+size_t adjacency_workspace(int dim, int64_t n, int64_t cap_cells);
 int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
               int count_index, int32_t *adj, int adj_cap, int32_t *deg,
-              int64_t *counters, cudaStream_t s);
+              int64_t *counters, void *ws, size_t ws_bytes, cudaStream_t s);
 int bar_blocks(int dim, int64_t n);
 int bar_sums(int dim, const float *P, int64_t n, const int32_t *adj,
              int adj_cap, const int32_t *deg, const dm_sizing *sz,
@@ -89,7 +90,7 @@ extern "C" {
 
 int dm_version(void) { return 10000; }
 const char *dm_last_error(void) { return dm::last_error(); }
-int dm_abi_count(void) { return 38; }
+int dm_abi_count(void) { return 39; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
   dmp::ExactScratch W;
@@ -145,12 +146,18 @@ int dm_cell_centroids(int32_t dim, const float *points, const int32_t *cells,
                             S(stream));
 }
 
+int dm_adjacency_workspace_size(int32_t dim, int64_t n, int64_t cap_cells,
+                                size_t *bytes) {
+  if (!bytes || (dim != 2 && dim != 3) || n < 0 || cap_cells < 0) return DM_ERR_ARG;
+  *bytes = dm::adjacency_workspace(dim, n, cap_cells);
+  return DM_OK;
+}
 int dm_adjacency(int32_t dim, int64_t n, const int32_t *cells,
                  int64_t cap_cells, int32_t count_index, int32_t *adj,
                  int32_t adj_cap, int32_t *deg, int64_t *counters,
-                 void *stream) {
+                 void *workspace, size_t workspace_bytes, void *stream) {
   return dm::adjacency(dim, n, cells, cap_cells, count_index, adj, adj_cap, deg,
-                       counters, S(stream));
+                       counters, workspace, workspace_bytes, S(stream));
 }
 
 int dm_unique_edges_workspace_size(int64_t n, int64_t m, size_t *bytes) {

@@ -87,11 +87,13 @@ DM_HD i128 det3_fx(int4 a, int4 b, int4 c) {
 }
 
 // det[a; b; c] for |coordinates| < 2^31 (differences of fixed coordinates)
-DM_HD i128 det3_fx_wide(const long long *a, const long long *b, const long long *c) {
-  i128 m0 = (i128)b[1] * c[2] - (i128)b[2] * c[1];
-  i128 m1 = (i128)b[2] * c[0] - (i128)b[0] * c[2];
-  i128 m2 = (i128)b[0] * c[1] - (i128)b[1] * c[0];
-  return a[0] * m0 + a[1] * m1 + a[2] * m2;
+DM_HD i128 det3_fx_wide(long long a0, long long a1, long long a2, long long b0,
+                        long long b1, long long b2, long long c0, long long c1,
+                        long long c2) {
+  i128 m0 = (i128)b1 * c2 - (i128)b2 * c1;
+  i128 m1 = (i128)b2 * c0 - (i128)b0 * c2;
+  i128 m2 = (i128)b0 * c1 - (i128)b1 * c0;
+  return a0 * m0 + a1 * m1 + a2 * m2;
 }
 
 DM_HD int sign128(i128 v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
@@ -176,20 +178,21 @@ DM_HD int insph3_fx_sos_tail(int4 a, int4 b, int4 c, int4 d) {
       case 3: s = -orient3_fx(a, b, d); break;
       case 2: s = orient3_fx(a, c, d); break;
       case 1: s = -orient3_fx(b, c, d); break;
-      case 0: {
-        long long X[3] = {(long long)b.x - a.x, (long long)b.y - a.y, (long long)b.z - a.z};
-        long long Y[3] = {(long long)c.x - a.x, (long long)c.y - a.y, (long long)c.z - a.z};
-        long long Q[3] = {(long long)d.x - a.x, (long long)d.y - a.y, (long long)d.z - a.z};
-        s = sign128(det3_fx_wide(X, Y, Q));
+      case 0:
+        s = sign128(det3_fx_wide((long long)b.x - a.x, (long long)b.y - a.y,
+                                 (long long)b.z - a.z, (long long)c.x - a.x,
+                                 (long long)c.y - a.y, (long long)c.z - a.z,
+                                 (long long)d.x - a.x, (long long)d.y - a.y,
+                                 (long long)d.z - a.z));
         break;
-      }
     }
     if (s) return s;
   }
   return 0;
 }
 
-DM_HD int insph3_fx_sos(int4 a, int4 b, int4 c, int4 d) {
+// out of line: the filters decide most calls, this keeps the kernels small
+DM_HD_NI int insph3_fx_sos(int4 a, int4 b, int4 c, int4 d) {
   int s = insph3_fx(a, b, c, d);
   return s ? s : insph3_fx_sos_tail(a, b, c, d);
 }
@@ -250,7 +253,7 @@ DM_HD int incirc2_fx_sos_tail(int4 a, int4 b, int4 c) {
   return 0;
 }
 
-DM_HD int incirc2_fx_sos(int4 a, int4 b, int4 c) {
+DM_HD_NI int incirc2_fx_sos(int4 a, int4 b, int4 c) {
   int s = incirc2_fx(a, b, c);
   return s ? s : incirc2_fx_sos_tail(a, b, c);
 }

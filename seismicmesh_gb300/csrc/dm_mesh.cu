@@ -113,82 +113,115 @@ __global__ void k_centroids(const float *P, const int32_t *cells, int64_t cap,
 // ---------------------------------------------------------------------------
 // adjacency: scatter every cell edge into both endpoint rows, then sort and
 // deduplicate each row in shared memory.
+// Adjacency rows from cells (replaces _get_edges + unique_edges of the
+// reference, generation/mesh_generator.py:680-688): CSR of the raw neighbour
+// lists (NV-1 entries per incident cell), then one warp per vertex sorts and
+// deduplicates its segment into a fixed-stride row.
 template <int NV>
-__global__ void k_adj_scatter(const int32_t *cells, int64_t cap_cells,
-                              const int64_t *counters, int count_index,
-                              int32_t *adj, int adj_cap, int32_t *deg,
-                              int64_t *counters_w) {
+__global__ void k_adj_count(const int32_t *cells, int64_t cap_cells,
+                            const int64_t *counters, int count_index, int32_t *cnt) {
   int64_t nc = min(counters[count_index], cap_cells);
-  bool ovf = false;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x)
+    for (int k = 0; k < NV; ++k) atomicAdd(&cnt[cells[NV * c + k]], NV - 1);
+}
+
+template <int NV>
+__global__ void k_adj_fill(const int32_t *cells, int64_t cap_cells,
+                           const int64_t *counters, int count_index,
+                           const int32_t *off, int32_t *cursor, int32_t *raw) {
+  int64_t nc = min(counters[count_index], cap_cells);
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
        c += (int64_t)gridDim.x * blockDim.x) {
     int v[NV];
     for (int k = 0; k < NV; ++k) v[k] = cells[NV * c + k];
-    for (int i = 0; i < NV; ++i)
-      for (int j = i + 1; j < NV; ++j) {
-        int a = v[i], b = v[j];
-        int sa = atomicAdd(&deg[a], 1);
-        if (sa < adj_cap) adj[(int64_t)a * adj_cap + sa] = b; else ovf = true;
-        int sb = atomicAdd(&deg[b], 1);
-        if (sb < adj_cap) adj[(int64_t)b * adj_cap + sb] = a; else ovf = true;
-      }
+    for (int i = 0; i < NV; ++i) {
+      int pos = off[v[i]] + atomicAdd(&cursor[v[i]], NV - 1);
+      for (int j = 0; j < NV; ++j)
+        if (j != i) raw[pos++] = v[j];
+    }
   }
-  if (ovf) flag_or(counters_w, DM_FLAG_ADJ_OVERFLOW);
 }
 
 constexpr int ADJ_WARPS = 8;
-constexpr int ADJ_MAXCAP = 128;
+constexpr int ADJ_SORTMAX = 1024;  // raw segment sorted in shared memory
 
-__global__ void __launch_bounds__(32 * ADJ_WARPS)
-    k_adj_sort(int64_t n, int32_t *adj, int adj_cap, int32_t *deg,
-               int64_t *counters) {
-  __shared__ int buf[ADJ_WARPS][ADJ_MAXCAP];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int *b = buf[w];
-  int size = 1;
-  while (size < adj_cap) size <<= 1;
-  unsigned long long ecount = 0;
-  for (int64_t v = (int64_t)blockIdx.x * ADJ_WARPS + w; v < n;
-       v += (int64_t)gridDim.x * ADJ_WARPS) {
-    int r = min(deg[v], adj_cap);
-    int32_t *row = adj + v * adj_cap;
-    for (int k = lane; k < size; k += 32) b[k] = k < r ? row[k] : 0x7fffffff;
-    __syncwarp();
-    // bitonic sort of `size` ints
-    for (int kk = 2; kk <= size; kk <<= 1)
-      for (int j = kk >> 1; j > 0; j >>= 1) {
-        for (int i = lane; i < size; i += 32) {
-          int ixj = i ^ j;
-          if (ixj > i) {
-            int x = b[i], y = b[ixj];
-            bool up = (i & kk) == 0;
-            if ((x > y) == up) {
-              b[i] = y;
-              b[ixj] = x;
-            }
+// bitonic sort of b[0..size) (size a power of two) by one warp
+__device__ __forceinline__ void warp_bitonic(int *b, int size, int lane) {
+  for (int kk = 2; kk <= size; kk <<= 1)
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < size; i += 32) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          int x = b[i], y = b[ixj];
+          bool up = (i & kk) == 0;
+          if ((x > y) == up) {
+            b[i] = y;
+            b[ixj] = x;
           }
         }
-        __syncwarp();
       }
-    // unique + compact
-    int base = 0;
-    for (int k0 = 0; k0 < r; k0 += 32) {
-      int k = k0 + lane;
-      bool keep = k < r && (k == 0 || b[k] != b[k - 1]);
-      unsigned m = __ballot_sync(0xffffffffu, keep);
-      int pos = base + __popc(m & ((1u << lane) - 1));
-      int val = keep ? b[k] : 0;
       __syncwarp();
-      if (keep) row[pos] = val;
-      base += __popc(m);
     }
+}
+
+__global__ void __launch_bounds__(32 * ADJ_WARPS)
+    k_adj_dedup(int64_t n, const int32_t *off, const int32_t *raw, int32_t *adj,
+                int adj_cap, int32_t *deg, int64_t *counters) {
+  __shared__ int buf[ADJ_WARPS][ADJ_SORTMAX];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int *b = buf[w];
+  unsigned long long ecount = 0;
+  bool ovf = false;
+  for (int64_t v = (int64_t)blockIdx.x * ADJ_WARPS + w; v < n;
+       v += (int64_t)gridDim.x * ADJ_WARPS) {
+    const int o = off[v], L = off[v + 1] - o;
+    int m;  // entries staged in b
+    if (L <= ADJ_SORTMAX) {
+      for (int k = lane; k < L; k += 32) b[k] = raw[o + k];
+      m = L;
+    } else {
+      // very high incidence: stage first occurrences only (quadratic scan)
+      m = 0;
+      for (int k0 = 0; k0 < L; k0 += 32) {
+        int k = k0 + lane;
+        int x = k < L ? raw[o + k] : 0;
+        bool first = k < L;
+        for (int j = 0; j < k0 + lane && first; ++j) first = raw[o + j] != x;
+        unsigned mk = __ballot_sync(0xffffffffu, first);
+        int pos = m + __popc(mk & ((1u << lane) - 1));
+        if (first && pos < ADJ_SORTMAX) b[pos] = x;
+        m += __popc(mk);
+      }
+      if (m > ADJ_SORTMAX) {
+        ovf = true;
+        m = ADJ_SORTMAX;
+      }
+    }
+    int size = 1;
+    while (size < m) size <<= 1;
+    for (int k = m + lane; k < size; k += 32) b[k] = 0x7fffffff;
     __syncwarp();
-    if (lane == 0) deg[v] = base;
+    warp_bitonic(b, size, lane);
+    // unique + compact into the row
+    int32_t *row = adj + v * adj_cap;
+    int base = 0;
+    for (int k0 = 0; k0 < m; k0 += 32) {
+      int k = k0 + lane;
+      bool keep = k < m && (k == 0 || b[k] != b[k - 1]);
+      unsigned mk = __ballot_sync(0xffffffffu, keep);
+      int pos = base + __popc(mk & ((1u << lane) - 1));
+      if (keep && pos < adj_cap) row[pos] = b[k];
+      base += __popc(mk);
+    }
+    if (base > adj_cap) ovf = true;
+    if (lane == 0) deg[v] = min(base, adj_cap);
     ecount += base;
+    __syncwarp();
   }
-  // unique edge count = half the sum of degrees (ecount is warp-uniform)
   if (lane == 0 && ecount)
     atomicAdd((unsigned long long *)&counters[DM_CNT_EDGES], ecount);
+  if (ovf && lane == 0) flag_or(counters, DM_FLAG_ADJ_OVERFLOW);
 }
 
 __global__ void k_half_edges(int64_t *counters) {
@@ -664,26 +697,57 @@ int cell_centroids(int dim, const float *P, const int32_t *cells, int64_t cap,
   return DM_OK;
 }
 
+static size_t carve_adj(Carve &c, int dim, int64_t n, int64_t cap_cells, int32_t **cnt,
+                        int32_t **off, int32_t **raw, int32_t **tmp) {
+  const int NV = dim + 1;
+  *cnt = c.take<int32_t>(n);
+  *off = c.take<int32_t>(n + 1);
+  *raw = c.take<int32_t>((size_t)NV * (NV - 1) * cap_cells);
+  *tmp = c.take<int32_t>(scan_tmp_elems(n));
+  return c.used;
+}
+
+size_t adjacency_workspace(int dim, int64_t n, int64_t cap_cells) {
+  Carve c(nullptr, 0);
+  int32_t *a, *b, *d, *e;
+  return carve_adj(c, dim, n, cap_cells, &a, &b, &d, &e) + 256;
+}
+
 int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
               int count_index, int32_t *adj, int adj_cap, int32_t *deg,
-              int64_t *counters, cudaStream_t s) {
+              int64_t *counters, void *ws, size_t ws_bytes, cudaStream_t s) {
   DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
-  DM_ARG_CHECK(adj_cap > 0 && adj_cap <= ADJ_MAXCAP, "adj_cap must be in 1..128");
+  DM_ARG_CHECK(adj_cap > 0, "adj_cap must be positive");
   DM_ARG_CHECK(count_index >= 0 && count_index < DM_NCOUNTERS, "count_index");
-  DM_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(int32_t) * n, s));
+  DM_ARG_CHECK(n >= 0 && n < (1 << 30) && cap_cells >= 0, "sizes");
+  DM_ARG_CHECK((dim + 1) * dim * cap_cells < (1ll << 31), "too many cells");
+  Carve c(ws, ws_bytes);
+  int32_t *cnt, *off, *raw, *tmp;
+  carve_adj(c, dim, n, cap_cells, &cnt, &off, &raw, &tmp);
+  if (!c.ok() || !ws) {
+    set_error("adjacency: workspace %zu < required %zu", ws_bytes, c.used);
+    return DM_ERR_WORKSPACE;
+  }
   DM_CUDA_TRY(cudaMemsetAsync(&counters[DM_CNT_EDGES], 0, sizeof(int64_t), s));
+  if (n == 0) return DM_OK;
+  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
   int nb = grid_for(cap_cells, 256);
   if (dim == 3)
-    k_adj_scatter<4><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index,
-                                        adj, adj_cap, deg, counters);
+    k_adj_count<4><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index, cnt);
   else
-    k_adj_scatter<3><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index,
-                                        adj, adj_cap, deg, counters);
+    k_adj_count<3><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index, cnt);
+  int rc = exclusive_scan_i32(cnt, off, n, tmp, s);
+  if (rc) return rc;
+  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
+  if (dim == 3)
+    k_adj_fill<4><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index, off, cnt, raw);
+  else
+    k_adj_fill<3><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index, off, cnt, raw);
   int nw = grid_for(n, ADJ_WARPS);
-  k_adj_sort<<<nw, 32 * ADJ_WARPS, 0, s>>>(n, adj, adj_cap, deg, counters);
+  k_adj_dedup<<<nw, 32 * ADJ_WARPS, 0, s>>>(n, off, raw, adj, adj_cap, deg, counters);
   k_half_edges<<<1, 1, 0, s>>>(counters);
   DM_LAUNCH_CHECK();
-  note_launches(3);
+  note_launches(7);
   return DM_OK;
 }
 

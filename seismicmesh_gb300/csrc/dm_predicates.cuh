@@ -251,6 +251,7 @@ struct ExactScratch {
   double w[3];
   double e2[2];
   double d3tmp[20];
+  double dx[4][3];  // exact differences of the FP64 filter stages
 };
 
 // orient3(a,b,c,d) = det3(b,c,d) - det3(a,c,d) + det3(a,b,d) - det3(a,b,c)
@@ -498,10 +499,10 @@ DM_HD int exact_diff(const float *b, const float *a, int dim, double *out) {
 
 // ---------------------------------------------------------------------------
 // Full predicates on raw coordinates (FP64 filter then exact).
-DM_HD int orient3_slow(const float *a, const float *b, const float *c,
+DM_HD_NI int orient3_slow(const float *a, const float *b, const float *c,
                           const float *d, ExactScratch *W) {
   DMP_COUNT(0);
-  double X[3], Y[3], Z[3];
+  double *X = W->dx[0], *Y = W->dx[1], *Z = W->dx[2];
   if (exact_diff(b, a, 3, X) && exact_diff(c, a, 3, Y) && exact_diff(d, a, 3, Z)) {
     int s = orient3_rel_filter<double>(X[0], X[1], X[2], Y[0], Y[1], Y[2], Z[0],
                                        Z[1], Z[2], 16.0 * DMP_U64);
@@ -516,18 +517,16 @@ DM_HD int orient3_slow(const float *a, const float *b, const float *c,
 
 DM_HD int orient3(const float *a, const float *b, const float *c,
                   const float *d, ExactScratch *W) {
-  float X[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
-  float Y[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
-  float Z[3] = {d[0] - a[0], d[1] - a[1], d[2] - a[2]};
-  int s = orient3_rel_filter<float>(X[0], X[1], X[2], Y[0], Y[1], Y[2], Z[0],
-                                    Z[1], Z[2], 16.0f * DMP_U32);
+  int s = orient3_rel_filter<float>(b[0] - a[0], b[1] - a[1], b[2] - a[2], c[0] - a[0],
+                                    c[1] - a[1], c[2] - a[2], d[0] - a[0], d[1] - a[1],
+                                    d[2] - a[2], 16.0f * DMP_U32);
   if (s) return s;
   return orient3_slow(a, b, c, d, W);
 }
 
-DM_HD int orient2_slow(const float *a, const float *b, const float *c,
+DM_HD_NI int orient2_slow(const float *a, const float *b, const float *c,
                           ExactScratch *W) {
-  double X[2], Y[2];
+  double *X = W->dx[0], *Y = W->dx[1];
   if (exact_diff(b, a, 2, X) && exact_diff(c, a, 2, Y)) {
     int s = orient2_rel_filter<double>(X[0], X[1], Y[0], Y[1], 8.0 * DMP_U64);
     if (s) return s;
@@ -537,20 +536,19 @@ DM_HD int orient2_slow(const float *a, const float *b, const float *c,
 
 DM_HD int orient2(const float *a, const float *b, const float *c,
                   ExactScratch *W) {
-  float X[2] = {b[0] - a[0], b[1] - a[1]};
-  float Y[2] = {c[0] - a[0], c[1] - a[1]};
-  int s = orient2_rel_filter<float>(X[0], X[1], Y[0], Y[1], 8.0f * DMP_U32);
+  int s = orient2_rel_filter<float>(b[0] - a[0], b[1] - a[1], c[0] - a[0], c[1] - a[1],
+                                    8.0f * DMP_U32);
   if (s) return s;
   return orient2_slow(a, b, c, W);
 }
 
 
 // unperturbed sign of insph3 (FP64 filter, then exact)
-DM_HD int insph3_slow(const float *a, const float *b, const float *c,
+DM_HD_NI int insph3_slow(const float *a, const float *b, const float *c,
                          const float *d, const float *e, int *overflow,
                          ExactScratch *W) {
   DMP_COUNT(2);
-  double X[3], Y[3], Z[3], Q[3];
+  double *X = W->dx[0], *Y = W->dx[1], *Z = W->dx[2], *Q = W->dx[3];
   if (exact_diff(b, a, 3, X) && exact_diff(c, a, 3, Y) && exact_diff(d, a, 3, Z) &&
       exact_diff(e, a, 3, Q)) {
     double wx = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
@@ -568,7 +566,7 @@ DM_HD int insph3_slow(const float *a, const float *b, const float *c,
 //   e: +o(a,b,c,d)  d: -o(a,b,c,e)  c: +o(a,b,d,e)  b: -o(a,c,d,e)  a: +o(b,c,d,e)
 // Points are visited from the lexicographically largest (largest
 // perturbation) down; the first non-zero coefficient decides.
-DM_HD int insph3_sos_tail(const float *a, const float *b, const float *c,
+DM_HD_NI int insph3_sos_tail(const float *a, const float *b, const float *c,
                           const float *d, const float *e, ExactScratch *W) {
   DMP_COUNT(4);
   int done = 0;  // bit mask of visited points
@@ -610,9 +608,9 @@ DM_HD int insph3_sos(const float *a, const float *b, const float *c,
   return insph3_sos_tail(a, b, c, d, e, W);
 }
 
-DM_HD int incirc2_slow(const float *a, const float *b, const float *c,
+DM_HD_NI int incirc2_slow(const float *a, const float *b, const float *c,
                           const float *d, int *overflow, ExactScratch *W) {
-  double X[2], Y[2], Z[2];
+  double *X = W->dx[0], *Y = W->dx[1], *Z = W->dx[2];
   if (exact_diff(b, a, 2, X) && exact_diff(c, a, 2, Y) && exact_diff(d, a, 2, Z)) {
     double wx = X[0] * X[0] + X[1] * X[1];
     double wy = Y[0] * Y[0] + Y[1] * Y[1];
@@ -625,7 +623,7 @@ DM_HD int incirc2_slow(const float *a, const float *b, const float *c,
 
 // perturbation coefficients of incirc2 (translated form):
 //   d: +o(a,b,c)  c: -o(a,b,d)  b: +o(a,c,d)  a: -o(b,c,d)
-DM_HD int incirc2_sos_tail(const float *a, const float *b, const float *c,
+DM_HD_NI int incirc2_sos_tail(const float *a, const float *b, const float *c,
                            const float *d, ExactScratch *W) {
   int done = 0;
   for (int step = 0; step < 4; ++step) {

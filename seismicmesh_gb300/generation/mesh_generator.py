@@ -30,7 +30,7 @@ from . import utils as mutils
 
 __all__ = ["sliver_removal", "generate_mesh"]
 
-ADJ_CAP = {2: 32, 3: 128}
+ADJ_CAP = {2: 32, 3: 64}
 
 
 def silence(func):
@@ -165,6 +165,7 @@ class _Engine:
         N.call("dm_delaunay_workspace_size", self.dim, self.n, ws)
         self.ws_dt = D.workspace(ws.value)
         self.adj = None
+        self.ws_adj = None
         nblk = N.c_int(0)
         N.call("dm_bar_blocks", self.n, nblk)
         self.nblk = nblk.value
@@ -230,15 +231,31 @@ class _Engine:
         self.counters[N.CNT_KEPT] = k
         return k
 
-    def build_adjacency(self):
-        if self.adj is None or self.adj.shape[0] != self.n:
+    def adjacency_async(self):
+        """dm_adjacency on the current stream, no host synchronisation"""
+        if self.adj is None or self.adj.shape != (self.n, self.adj_cap):
             self.adj = D.empty((self.n, self.adj_cap), torch.int32)
             self.deg = D.empty((self.n,), torch.int32)
+        ws = N.c_sz(0)
+        N.call("dm_adjacency_workspace_size", self.dim, self.n, self.cap_cells, ws)
+        if self.ws_adj is None or self.ws_adj.numel() < ws.value:
+            self.ws_adj = D.workspace(ws.value)
         N.call(
             "dm_adjacency", self.dim, self.n, D.ptr(self.kept), self.cap_cells, N.CNT_KEPT,
             D.ptr(self.adj), self.adj_cap, D.ptr(self.deg), D.ptr(self.counters),
-            D.stream_ptr(),
+            D.ptr(self.ws_adj), self.ws_adj.numel(), D.stream_ptr(),
         )
+
+    def build_adjacency(self):
+        """Adjacency rows; widens the rows when a vertex has more neighbours
+        than the row stride."""
+        while True:
+            self.adjacency_async()
+            flags = int(self.counters[N.CNT_FLAGS].item())
+            if not flags & N.FLAG_ADJ_OVERFLOW:
+                return
+            self.counters[N.CNT_FLAGS] = flags & ~N.FLAG_ADJ_OVERFLOW
+            self.adj_cap *= 2
 
     def slot_sizes(self, sizing):
         """per adjacency slot h(midpoint) for host-callable sizing functions"""

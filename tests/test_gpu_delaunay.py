@@ -171,3 +171,83 @@ def test_grid_aligned_points_match_qhull(cuda, dim, n):
     assert np.array_equal(eng.P[:, :dim].cpu().numpy().astype(np.float64), p)
     nc = eng.triangulate()
     dc.assert_same_triangulation(p, eng.cells[:nc].cpu().numpy())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["random", "hub"])
+def test_adjacency_rows_match_unique_edges(cuda, case):
+    """dm_adjacency rows are the sorted unique neighbours from the cells
+    (_get_edges + unique_edges of the reference); a hub vertex with more
+    neighbours than the row stride widens the rows instead of dropping
+    neighbours."""
+    rng = np.random.default_rng(23)
+    if case == "random":
+        p = rng.uniform(-1, 1, (5000, 3))
+    else:
+        # 80 neighbours: 156 star cells, within the star capacity (192 cells)
+        s = rng.standard_normal((80, 3))
+        p = np.vstack([[0.0, 0.0, 0.0], s / np.linalg.norm(s, axis=1)[:, None]])
+    p = p.astype(np.float32).astype(np.float64)
+    eng = _Engine(3, p, 0, grid=False)
+    nc = eng.triangulate()
+    eng.kept[:nc] = eng.cells[:nc]
+    eng.counters[N.CNT_KEPT] = nc
+    eng.build_adjacency()
+    cells = eng.cells[:nc].cpu().numpy()
+    e = np.concatenate([cells[:, [i, j]] for i in range(4) for j in range(i + 1, 4)])
+    e = np.unique(np.sort(e, axis=1), axis=0)
+    nbr = [[] for _ in range(len(p))]
+    for a, b in e:
+        nbr[a].append(b)
+        nbr[b].append(a)
+    deg = eng.deg.cpu().numpy()
+    adj = eng.adj.cpu().numpy()
+    for v in range(len(p)):
+        assert deg[v] == len(nbr[v]), (v, deg[v], len(nbr[v]))
+        assert np.array_equal(adj[v, : deg[v]], np.sort(nbr[v])), v
+    assert int(eng.counters[N.CNT_EDGES].item()) == len(e)
+    if case == "hub":
+        assert deg[0] == 80 and eng.adj_cap >= 80
+
+
+@pytest.mark.gpu
+def test_device_predicates_match_host_exact_predicates(cuda):
+    """The floating-point exact stages on the device (FP32 filter, FP64
+    filter, expansion arithmetic, symbolic perturbation) give the host's
+    signs on near-degenerate and exactly degenerate 5-point tuples."""
+    import ctypes
+
+    L = N.lib()
+    f = L.dmdbg_predicates
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    rng = np.random.default_rng(29)
+    pts = []
+    # cospherical points (on a sphere up to float rounding), a jittered
+    # lattice and an exact lattice with a non-representable offset
+    s = rng.standard_normal((400, 3))
+    pts.append(0.3 + 0.7 * s / np.linalg.norm(s, axis=1)[:, None])
+    g = np.stack(np.meshgrid(*[np.arange(4) * 0.1] * 3, indexing="ij"), -1).reshape(-1, 3)
+    pts.append(0.2 + g + 1e-7 * rng.standard_normal(g.shape))
+    pts.append(1e-9 + g)
+    P = np.concatenate(pts).astype(np.float32)
+    n = len(P)
+    lat0 = n - len(g)  # the exact lattice block: coplanar and cospherical tuples
+    tup = np.concatenate([rng.integers(0, n, (3000, 5)), rng.integers(lat0, n, (3000, 5))]).astype(np.int32)
+    tup = tup[np.array([len(set(t)) == 5 for t in tup])]
+    P4 = np.zeros((n, 4), np.float32)
+    P4[:, :3] = P
+    Pd = torch.from_numpy(P4).cuda()
+    Td = torch.from_numpy(tup).cuda()
+    fp = N.fptr
+    o_host = np.array([L.dm_orient3(*[fp(np.ascontiguousarray(P[i])) for i in t[:4]]) for t in tup])
+    for kind in (0, 3, 4):
+        out = torch.empty(len(tup), dtype=torch.int32, device="cuda")
+        assert f(Pd.data_ptr(), Td.data_ptr(), len(tup), kind, out.data_ptr(), None) == 0
+        np.testing.assert_array_equal(out.cpu().numpy(), o_host)
+    nz = o_host != 0
+    s_host = np.array([L.dm_insphere_sos(*[fp(np.ascontiguousarray(P[i])) for i in t]) for t in tup[nz]])
+    out = torch.empty(int(nz.sum()), dtype=torch.int32, device="cuda")
+    Tn = torch.from_numpy(np.ascontiguousarray(tup[nz])).cuda()
+    assert f(Pd.data_ptr(), Tn.data_ptr(), int(nz.sum()), 1, out.data_ptr(), None) == 0
+    np.testing.assert_array_equal(out.cpu().numpy(), s_host)
+    assert (o_host == 0).sum() > 50  # exact degeneracies were exercised
