@@ -387,12 +387,9 @@ __device__ __forceinline__ void warp_argmin(float &key, int &j, int &gid) {
 }
 
 // ---- 3D level-1 predicates on shared candidates (p is the origin)
-__device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
-                                   int a, int b, int c, dmp::ExactScratch *W) {
-  float4 A = S.c[a], B = S.c[b], C = S.c[c];
-  int s = dmp::orient3_rel_filter<float>(A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
-                                         C.z, 16.0f * DMP_U32);
-  if (s) return s;
+// exact orient3(p, a, b, c) once the filter has failed
+__device__ __forceinline__ int o3L_exact(const WarpL1<3> &S, const float *P, int ip,
+                                         int a, int b, int c, dmp::ExactScratch *W) {
   const int4 IA = S.ci[a], IB = S.ci[b], IC = S.ci[c];
   if (IA.w & IB.w & IC.w) return dmp::orient3_fx(IA, IB, IC);
   float pr[3], ar[3], br[3], cr[3];
@@ -403,6 +400,57 @@ __device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
   return dmp::orient3_slow(pr, ar, br, cr, W);
 }
 
+__device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
+                                   int a, int b, int c, dmp::ExactScratch *W) {
+  float4 A = S.c[a], B = S.c[b], C = S.c[c];
+  int s = dmp::orient3_rel_filter<float>(A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
+                                         C.z, 16.0f * DMP_U32);
+  if (s) return s;
+  return o3L_exact(S, P, ip, a, b, c, W);
+}
+
+// sign of det with |error| <= c * perm; 0 when undecided (including
+// overflow, underflow and NaN, which go to the exact stages)
+__device__ __forceinline__ int filter_sign(float det, float perm, float c) {
+  if (!(perm < 1e30f) || !(perm >= 1e-30f)) return 0;
+  float err = c * perm;
+  return det > err ? 1 : (det < -err ? -1 : 0);
+}
+
+// 3x3 determinant of rows (a, b, c) and its permanent
+__device__ __forceinline__ float det3p(float a0, float a1, float a2, float b0, float b1,
+                                       float b2, float c0, float c1, float c2, float &perm) {
+  float m0 = b1 * c2 - b2 * c1, m1 = b2 * c0 - b0 * c2, m2 = b0 * c1 - b1 * c0;
+  float p0 = fabsf(b1 * c2) + fabsf(b2 * c1), p1 = fabsf(b2 * c0) + fabsf(b0 * c2),
+        p2 = fabsf(b0 * c1) + fabsf(b1 * c0);
+  perm = fabsf(a0) * p0 + fabsf(a1) * p1 + fabsf(a2) * p2;
+  return a0 * m0 + a1 * m1 + a2 * m2;
+}
+
+// insph3(p, a, b, c, y) for a fixed (a, b, c) and many y: expansion along
+// the row of y, det = -y.x Mx + y.y My - y.z Mz + y.w Mw, with the 3x3
+// minors of rows (a, b, c).  With FP32 inputs (relative coordinates and
+// lifts rounded once) the error is below 17u * sum |y_k| perm(M_k); the
+// filter uses 48u.
+struct SphereRows {
+  float mx, my, mz, mw, px, py, pz, pw;
+};
+__device__ __forceinline__ void sphere_rows(SphereRows &R, float4 A, float4 B, float4 C) {
+  R.mx = det3p(A.y, A.z, A.w, B.y, B.z, B.w, C.y, C.z, C.w, R.px);
+  R.my = det3p(A.x, A.z, A.w, B.x, B.z, B.w, C.x, C.z, C.w, R.py);
+  R.mz = det3p(A.x, A.y, A.w, B.x, B.y, B.w, C.x, C.y, C.w, R.pz);
+  R.mw = det3p(A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y, C.z, R.pw);
+}
+__device__ __forceinline__ int sphere_filter(const SphereRows &R, float4 Y) {
+  float det = -Y.x * R.mx + Y.y * R.my - Y.z * R.mz + Y.w * R.mw;
+  float perm = fabsf(Y.x) * R.px + fabsf(Y.y) * R.py + fabsf(Y.z) * R.pz + fabsf(Y.w) * R.pw;
+  return filter_sign(det, perm, 48.0f * DMP_U32);
+}
+
+__device__ __forceinline__ int is3L_exact(const WarpL1<3> &S, const float *P, int ip,
+                                          int a, int b, int c, int d, int &ovf,
+                                          dmp::ExactScratch *W);
+
 __device__ __forceinline__ int is3L(const WarpL1<3> &S, const float *P, int ip,
                                     int a, int b, int c, int d, int &ovf,
                                     dmp::ExactScratch *W) {
@@ -412,6 +460,13 @@ __device__ __forceinline__ int is3L(const WarpL1<3> &S, const float *P, int ip,
   int s = dmp::insph3_rel_filter<float>(X, Y, Z, Q, A.w, B.w, C.w, D.w,
                                         48.0f * DMP_U32);
   if (s) return s;
+  return is3L_exact(S, P, ip, a, b, c, d, ovf, W);
+}
+
+// exact perturbed insph3(p, a, b, c, d) once the filter has failed
+__device__ __forceinline__ int is3L_exact(const WarpL1<3> &S, const float *P, int ip,
+                                          int a, int b, int c, int d, int &ovf,
+                                          dmp::ExactScratch *W) {
   const int4 IA = S.ci[a], IB = S.ci[b], IC = S.ci[c], ID = S.ci[d];
   if (IA.w & IB.w & IC.w & ID.w) return dmp::insph3_fx_sos(IA, IB, IC, ID);
   float pr[3], ar[3], br[3], cr[3], dr[3];
@@ -438,6 +493,10 @@ __device__ __forceinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
   float inv = nn > 0.f ? 0.5f / nn : 0.f;
   float cx = (ty * nz - tz * ny) * inv, cy = (tz * nx - tx * nz) * inv,
         cz = (tx * ny - ty * nx) * inv;
+  // orientation of every candidate against the face: Y . (A x B), with the
+  // permanent terms of A x B for the error bound (16u, as orient3 filters)
+  const float pnx = fabsf(A.y * B.z) + fabsf(A.z * B.y), pny = fabsf(A.z * B.x) + fabsf(A.x * B.z),
+              pnz = fabsf(A.x * B.y) + fabsf(A.y * B.x);
   uint32_t pos = 0;
   float bk = FLT_MAX;
   int bj = -1, bg = 0x7fffffff;
@@ -445,10 +504,13 @@ __device__ __forceinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
   for (int s = 0; s < L1<3>::PER; ++s) {
     int j = lane + 32 * s;
     if (j < nc && j != a && j != b) {
-      if (o3L(S, P, ip, a, b, j, W) > 0) {
+      float4 Y = S.c[j];
+      float den = Y.x * nx + Y.y * ny + Y.z * nz;
+      int o = filter_sign(den, fabsf(Y.x) * pnx + fabsf(Y.y) * pny + fabsf(Y.z) * pnz,
+                          16.0f * DMP_U32);
+      if (o == 0) o = o3L_exact(S, P, ip, a, b, j, W);
+      if (o > 0) {
         pos |= 1u << s;
-        float4 Y = S.c[j];
-        float den = Y.x * nx + Y.y * ny + Y.z * nz;
         float tau = (Y.w - 2.f * (Y.x * cx + Y.y * cy + Y.z * cz)) / den;
         if (!(tau == tau) || !(den > 0.f)) tau = FLT_MAX;
         int g = S.id[j];
@@ -462,13 +524,18 @@ __device__ __forceinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
   }
   warp_argmin(bk, bj, bg);
   if (bj < 0) return -1;
+  // verification: no positive candidate inside the sphere (p, a, b, bj)
   for (int it = 0; it < nc + 1; ++it) {
+    SphereRows R;
+    sphere_rows(R, A, B, S.c[bj]);
     int found = -1;
 #pragma unroll
     for (int s = 0; s < L1<3>::PER; ++s) {
       int j = lane + 32 * s;
       if (found < 0 && (pos >> s & 1u) && j != bj) {
-        if (is3L(S, P, ip, a, b, bj, j, ovf, W) < 0) found = j;
+        int v = sphere_filter(R, S.c[j]);
+        if (v == 0) v = is3L_exact(S, P, ip, a, b, bj, j, ovf, W);
+        if (v < 0) found = j;
       }
     }
     unsigned m = __ballot_sync(0xffffffffu, found >= 0);
@@ -697,10 +764,15 @@ __device__ __forceinline__ bool empty3L(const WarpL1<3> &S, const float *P, int 
                                         uint32_t tr, int lane, int &ovf,
                                         dmp::ExactScratch *W) {
   int a = un0(tr), b = un1(tr), c = un2(tr);
+  SphereRows R;
+  sphere_rows(R, S.c[a], S.c[b], S.c[c]);
   bool inside = false;
   for (int j = lane; j < S.nc; j += 32)
-    if (!inside && j != a && j != b && j != c)
-      inside = is3L(S, P, ip, a, b, c, j, ovf, W) < 0;
+    if (!inside && j != a && j != b && j != c) {
+      int v = sphere_filter(R, S.c[j]);
+      if (v == 0) v = is3L_exact(S, P, ip, a, b, c, j, ovf, W);
+      inside = v < 0;
+    }
   return !__any_sync(0xffffffffu, inside);
 }
 
