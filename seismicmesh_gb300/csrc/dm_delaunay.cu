@@ -67,6 +67,7 @@ struct DTArgs {
   int32_t *blk_cnt;   // [cap_blocks]
   float *blk_box;     // [cap_blocks * 6]
   uint8_t *dup;       // [n]
+  float4 *spts;       // [n] points in cell order: x, y, z, id bits (-1: duplicate)
   int32_t *esc;       // [n]
   int4 *esc_seed;     // [n]
   int32_t *cells;
@@ -92,6 +93,7 @@ static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
   a.blk_cnt = c.take<int32_t>(a.cap_blocks);
   a.blk_box = c.take<float>(a.cap_blocks * 6);
   a.dup = c.take<uint8_t>(n);
+  a.spts = c.take<float4>(n);
   a.esc = c.take<int32_t>(n);
   a.esc_seed = c.take<int4>(n);
   return c.used;
@@ -300,6 +302,19 @@ __global__ void k_cell_sort(const float *P, const GridParams *gp,
       atomicAdd((unsigned long long *)&counters[DM_CNT_DUPS], (unsigned long long)ndup);
       flag_or(counters, DM_FLAG_DUPLICATES);
     }
+  }
+}
+
+// cell-ordered copy of the points: one 16-byte load per visited point
+template <int DIM>
+__global__ void k_sorted_points(const float *P, int64_t n, const int32_t *sorted,
+                                const uint8_t *dup, float4 *spts) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int j = sorted[i];
+    float x[3] = {0.f, 0.f, 0.f};
+    load_pt<DIM>(P, j, x);
+    spts[i] = make_float4(x[0], x[1], x[2], __int_as_float(dup[j] ? -1 : j));
   }
 }
 
@@ -684,10 +699,10 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
         continue;
       int c = x + g.dims[0] * (y + g.dims[1] * z);
       for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) {
-        int q = A.sorted[i];
-        if (q == ip || A.dup[q]) continue;
-        float xq[3];
-        load_pt<DIM>(A.P, q, xq);
+        const float4 sq = A.spts[i];
+        int q = __float_as_int(sq.w);
+        if (q == ip || q < 0) continue;
+        float xq[3] = {sq.x, sq.y, sq.z};
         float d2s = 0.f;
         for (int k = 0; k < DIM; ++k) {
           float dd = xq[k] - px[k];
@@ -731,10 +746,10 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
       continue;
     int c = x + g.dims[0] * (y + g.dims[1] * z);
     for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) {
-      int q = A.sorted[i];
-      if (q == ip || A.dup[q]) continue;
-      float xq[3];
-      load_pt<DIM>(A.P, q, xq);
+      const float4 sq = A.spts[i];
+      int q = __float_as_int(sq.w);
+      if (q == ip || q < 0) continue;
+      float xq[3] = {sq.x, sq.y, sq.z};
       float r[3] = {0, 0, 0}, d2s = 0.f;
       for (int k = 0; k < DIM; ++k) {
         r[k] = xq[k] - px[k];
@@ -1336,12 +1351,11 @@ __device__ __forceinline__ int insph_face3(const Face3 &F, const float *c, const
 }
 
 __device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j,
-                                          int &best, float *bx, int &ovf,
+                                          float4 q, int &best, float *bx, int &ovf,
                                           dmp::ExactScratch *W) {
-  if (j == F.ip || j == F.ia || j == F.ib || A.dup[j]) return;
+  if (j == F.ip || j == F.ia || j == F.ib) return;
   L2S_ADD(3, 1);
-  float y[3];
-  load_pt<3>(A.P, j, y);
+  float y[3] = {q.x, q.y, q.z};
   if (side3(F, y, W) <= 0) return;
   if (best < 0 || insph_face3(F, bx, y, ovf, W) < 0) {
     best = j;
@@ -1389,7 +1403,12 @@ __device__ __forceinline__ void cell_range(const GridParams &g, double c, double
 // the points of cell c
 template <typename F>
 __device__ __forceinline__ void for_cell(const DTArgs &A, int c, F f) {
-  for (int i = A.cell_start[c]; i < A.cell_start[c + 1]; ++i) f(A.sorted[i]);
+  const int e = A.cell_start[c + 1];
+  for (int i = A.cell_start[c]; i < e; ++i) {
+    const float4 q = A.spts[i];
+    const int j = __float_as_int(q.w);
+    if (j >= 0) f(j, q);  // duplicates are skipped
+  }
 }
 
 // Search region of a gift-wrap query on face (p, a, b) with current winner y:
@@ -1591,7 +1610,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   auto scan_cell = [&](int x, int y, int z) {
     if (x >= 0 && y >= 0 && z >= 0 && x < g.dims[0] && y < g.dims[1] && z < g.dims[2])
       for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-               [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
+               [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
   };
   // local search: the 27 cells around the face centroid
   if (lane < 27) scan_cell(cc[0] + lane % 3 - 1, cc[1] + (lane / 3) % 3 - 1, cc[2] + lane / 9 - 1);
@@ -1654,7 +1673,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
         float bhi[3] = {blo[0] + g.cs, blo[1] + g.cs, blo[2] + g.cs};
         if (!region_hits3(R, blo, bhi)) continue;
         for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                 [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
+                 [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
       }
     } else {
       int blo[3], bhi[3];
@@ -1676,7 +1695,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
             for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
               if (cheb3(cc, x, y, z) <= rex) continue;
               for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                       [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
+                       [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
             }
       }
     }
@@ -1693,7 +1712,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
           for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
             if (cheb3(cc, x, y, z) <= rex) continue;
             for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                     [&](int j) { consider3(A, F, j, best, bx, ovf, W); });
+                     [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
           }
     }
   }
@@ -1779,11 +1798,10 @@ __device__ __forceinline__ int cmp2(const Edge2 &E, const float *bx,
 }
 
 __device__ __forceinline__ void consider2(const DTArgs &A, const Edge2 &E, int j,
-                                          int &best, float *bx, int &ovf,
+                                          float4 q, int &best, float *bx, int &ovf,
                                           dmp::ExactScratch *W) {
-  if (j == E.ip || j == E.ix || A.dup[j]) return;
-  float y[2];
-  load_pt<2>(A.P, j, y);
+  if (j == E.ip || j == E.ix) return;
+  float y[2] = {q.x, q.y};
   if (side2(E, y, W) <= 0) return;
   if (best < 0 || cmp2(E, bx, y, ovf, W) < 0) {
     best = j;
@@ -1830,7 +1848,7 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
   if (lane < 9) {
     int x = cc[0] + lane % 3 - 1, y = cc[1] + lane / 3 - 1;
     if (x >= 0 && y >= 0 && x < g.dims[0] && y < g.dims[1])
-      for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
+      for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
   }
   best = tourney2(A, E, best, ovf, W);
   // Search region (as in gq3): a point beating the winner y lies inside
@@ -1894,7 +1912,7 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
           dd += e * e;
         }
         if (dd > r2 + 1e-6f * g.cs * g.cs) continue;
-        for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
+        for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
       }
     } else {
       int blo[2] = {lo[0] / g.bs, lo[1] / g.bs}, bhi[2] = {hi[0] / g.bs, hi[1] / g.bs};
@@ -1915,7 +1933,7 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
         for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
           for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
             if (in_local(cc, x, y, 0, 2)) continue;
-            for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
+            for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
           }
       }
     }
@@ -1936,7 +1954,7 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
       for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
         for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
           if (in_local(cc, x, y, 0, 2)) continue;
-          for_cell(A, x + g.dims[0] * y, [&](int j) { consider2(A, E, j, best, bx, ovf, W); });
+          for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
         }
     }
   }
@@ -2537,10 +2555,12 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   int ncb = grid_for(a.cap_cells, 256);
   if (dim == 3) {
     k_cell_sort<3><<<ncb, 256, 0, s>>>(pts, a.gp, a.cell_start, a.sorted, a.dup, counters);
+    k_sorted_points<3><<<nb, 256, 0, s>>>(pts, n, a.sorted, a.dup, a.spts);
     k_block_boxes<3><<<grid_for(a.cap_blocks, 128), 128, 0, s>>>(
         pts, a.gp, a.cell_start, a.sorted, a.blk_cnt, a.blk_box);
   } else {
     k_cell_sort<2><<<ncb, 256, 0, s>>>(pts, a.gp, a.cell_start, a.sorted, a.dup, counters);
+    k_sorted_points<2><<<nb, 256, 0, s>>>(pts, n, a.sorted, a.dup, a.spts);
     k_block_boxes<2><<<grid_for(a.cap_blocks, 128), 128, 0, s>>>(
         pts, a.gp, a.cell_start, a.sorted, a.blk_cnt, a.blk_box);
   }
