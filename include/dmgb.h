@@ -276,6 +276,19 @@ int dm_limgrad(const int32_t *dims_host, double elen, double dfdx,
  * gradient_term if grad>0), hmin, hmax), then the Courant bound when
  * dt, cr_max and space_order are non-zero.  gradient_term may be NULL when
  * grad == 0.  workspace: >= 4 bytes of device memory. */
+/* Gradient sizing term (_gradient_sizing, sizing/mesh_size_function.py:
+ * 428-448): grad / (v + 0.1) with v the windowed variance of vp (box means
+ * of vp and vp^2 as scipy.ndimage.uniform_filter: per-axis window
+ * window_host[k], origin 0, 'reflect' boundaries), divided by its maximum and
+ * shifted by its minimum.  vp is a C-order float64 grid of dims_host[0..dim)
+ * read with the unit scale and water replacement of dm_size_from_velocity
+ * (replace != 0: values below 1e-3 become vp_water).  The result feeds
+ * gradient_term of dm_size_from_velocity.  FP64 running sums per grid line. */
+int dm_gradient_term_workspace_size(int64_t n, size_t *bytes);
+int dm_gradient_term(const double *vp, const int32_t *dims_host, int32_t dim,
+                     const int32_t *window_host, double scale, double vp_water,
+                     int32_t replace, double grad, double *gradient_term,
+                     void *workspace, size_t workspace_bytes, void *stream);
 int dm_size_from_velocity(double *vp, int64_t n, int64_t row_len,
                           const double *gradient_term, double scale,
                           double vp_water, double wl, double freq, double grad,

@@ -80,6 +80,12 @@ SIGNATURES = {
     ),
     "dm_cell_centroids": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
     "dm_adjacency_workspace_size": (c_int, [c_int, c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_gradient_term_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_gradient_term": (
+        c_int,
+        [c_p, ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int), c_d, c_d, c_int, c_d, c_p,
+         c_p, c_sz, c_p],
+    ),
     "dm_adjacency": (c_int, [c_int, c_i64, c_p, c_i64, c_int, c_p, c_int, c_p, c_p, c_p, c_sz, c_p]),
     "dm_unique_edges_workspace_size": (c_int, [c_i64, c_i64, ctypes.POINTER(c_sz)]),
     "dm_unique_edges": (c_int, [c_p, c_i64, c_i64, c_p, ctypes.POINTER(c_i64), c_p, c_sz, c_p]),

@@ -50,6 +50,10 @@ size_t sliver_workspace(int64_t n_points);
 int limgrad(const int32_t *dims, double elen, double dfdx, int imax, double *f,
             cudaStream_t s);
 int unique_edges_workspace(int64_t n, int64_t m, size_t *bytes);
+size_t gradient_term_workspace(int64_t n);
+int gradient_term(const double *vp, const int32_t *dims, int dim, const int32_t *window,
+                  double scale, double vp_water, int replace, double grad, double *g,
+                  void *ws, size_t ws_bytes, cudaStream_t s);
 int unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
                  int64_t *n_out, void *ws, size_t ws_bytes, cudaStream_t s);
 int unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
@@ -90,7 +94,7 @@ extern "C" {
 
 int dm_version(void) { return 10000; }
 const char *dm_last_error(void) { return dm::last_error(); }
-int dm_abi_count(void) { return 39; }
+int dm_abi_count(void) { return 41; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
   dmp::ExactScratch W;
@@ -173,6 +177,19 @@ int dm_unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
 int dm_unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
                             int32_t *out, int64_t *n_out_host, void *stream) {
   return dm::unique_edges_noalloc(edges, m, n, out, n_out_host, S(stream));
+}
+
+int dm_gradient_term_workspace_size(int64_t n, size_t *bytes) {
+  if (!bytes || n < 0) return DM_ERR_ARG;
+  *bytes = dm::gradient_term_workspace(n);
+  return DM_OK;
+}
+int dm_gradient_term(const double *vp, const int32_t *dims_host, int32_t dim,
+                     const int32_t *window_host, double scale, double vp_water,
+                     int32_t replace, double grad, double *gradient_term,
+                     void *workspace, size_t workspace_bytes, void *stream) {
+  return dm::gradient_term(vp, dims_host, dim, window_host, scale, vp_water, replace,
+                           grad, gradient_term, workspace, workspace_bytes, S(stream));
 }
 
 int dm_bar_blocks(int64_t n, int32_t *nblk) {

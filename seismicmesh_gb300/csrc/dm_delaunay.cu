@@ -52,6 +52,10 @@ struct GridParams {
 
 constexpr int kNoFix = -100000;
 
+// level-3 star storage: per-warp slots in the workspace
+constexpr int L3_CAP_TRI = 4096, L3_CAP_OPEN = 2048, L3_WARPS = 4, L3_BLOCKS = 76;
+constexpr int kCntL3 = 11;  // counters slot: stars deferred to level 3
+
 struct DTArgs {
   int dim;
   int64_t n;
@@ -68,6 +72,9 @@ struct DTArgs {
   float *blk_box;     // [cap_blocks * 6]
   uint8_t *dup;       // [n]
   float4 *spts;       // [n] points in cell order: x, y, z, id bits (-1: duplicate)
+  int32_t *l3_list;   // [n] escalated stars deferred to level 3
+  int3 *l3_tri, *l3_open;  // level-3 star storage, one slot per warp
+  int32_t *l3_cnt;
   int32_t *esc;       // [n]
   int4 *esc_seed;     // [n]
   int32_t *cells;
@@ -94,6 +101,10 @@ static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
   a.blk_box = c.take<float>(a.cap_blocks * 6);
   a.dup = c.take<uint8_t>(n);
   a.spts = c.take<float4>(n);
+  a.l3_list = c.take<int32_t>(n);
+  a.l3_tri = c.take<int3>((size_t)L3_BLOCKS * L3_WARPS * L3_CAP_TRI);
+  a.l3_open = c.take<int3>((size_t)L3_BLOCKS * L3_WARPS * L3_CAP_OPEN);
+  a.l3_cnt = c.take<int32_t>((size_t)L3_BLOCKS * L3_WARPS * 4);
   a.esc = c.take<int32_t>(n);
   a.esc_seed = c.take<int4>(n);
   return c.used;
@@ -2237,9 +2248,21 @@ __device__ __forceinline__ bool gseed2(WarpL1<2> &Q, const DTArgs &A, const Grid
   return false;
 }
 
-__device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane) {
+// Storage of one star under construction: link triangles, open link edges
+// (3D) and counters cnt = {ntri, nopen, flags}.  Level 2 keeps it in shared
+// memory (192 triangles); stars that outgrow it are finished by level 3 in a
+// per-warp slot of global memory (L3_CAP_TRI triangles).
+struct StarStore {
+  int3 *tri, *open;
+  int *cnt;
+  int cap_tri, cap_open;
+};
+
+
+__device__ __forceinline__ int find_rev_s(const StarStore &S, int s, int t, int lane) {
+  const int nopen = S.cnt[1];
   int hit = -1;
-  for (int k = lane; k < S.nopen; k += 32) {
+  for (int k = lane; k < nopen; k += 32) {
     int3 e = S.open[k];
     if (e.x == t && e.y == s) hit = k;
   }
@@ -2248,237 +2271,344 @@ __device__ __forceinline__ int find_rev2(const WarpL2 &S, int s, int t, int lane
   return __shfl_sync(0xffffffffu, hit, __ffs(m) - 1);
 }
 
+// exhaustive gift-wrap walk of the star of ip (3D) from a seed link triangle;
+// false when the storage overflowed
+__device__ __forceinline__ bool walk3(const DTArgs &A, const GridParams &g, int ip, int3 seed,
+                                      int lane, int &ovf, dmp::ExactScratch *W,
+                                      const StarStore &S) {
+  if (lane == 0) {
+    S.cnt[0] = 1;
+    S.tri[0] = seed;
+    S.open[0] = make_int3(seed.x, seed.y, seed.z);
+    S.open[1] = make_int3(seed.y, seed.z, seed.x);
+    S.open[2] = make_int3(seed.z, seed.x, seed.y);
+    S.cnt[1] = 3;
+    S.cnt[2] = 0;
+  }
+  __syncwarp();
+  while (S.cnt[1] > 0) {
+    int3 e = S.open[S.cnt[1] - 1];
+    __syncwarp();
+    if (lane == 0) S.cnt[1]--;
+    __syncwarp();
+    int u = e.x, v = e.y;
+    int y = gq3(A, g, ip, v, u, lane, ovf, W);
+    if (y < 0) continue;  // convex-hull face
+    if (S.cnt[0] >= S.cap_tri) {
+      if (lane == 0) S.cnt[2] |= 1;
+      __syncwarp();
+      break;
+    }
+    if (lane == 0) S.tri[S.cnt[0]++] = make_int3(v, u, y);
+    __syncwarp();
+    int es[2][3] = {{u, y, v}, {y, v, u}};
+    for (int q = 0; q < 2; ++q) {
+      int r = find_rev_s(S, es[q][0], es[q][1], lane);
+      if (lane == 0) {
+        if (r >= 0) {
+          S.open[r] = S.open[S.cnt[1] - 1];
+          S.cnt[1]--;
+        } else if (S.cnt[1] < S.cap_open) {
+          S.open[S.cnt[1]++] = make_int3(es[q][0], es[q][1], es[q][2]);
+        } else {
+          S.cnt[2] |= 1;
+        }
+      }
+      __syncwarp();
+    }
+    if (S.cnt[2]) break;
+  }
+  __syncwarp();
+  return S.cnt[2] == 0;
+}
+
+// cells of a finished star owned by ip (smallest index)
+__device__ __forceinline__ void emit3(const DTArgs &A, int ip, const StarStore &S, int lane) {
+  const int ntri = S.cnt[0];
+  for (int t0 = 0; t0 < ntri; t0 += 32) {
+    int t = t0 + lane;
+    bool own = false;
+    int3 tr = make_int3(0, 0, 0);
+    if (t < ntri) {
+      tr = S.tri[t];
+      own = ip < tr.x && ip < tr.y && ip < tr.z;
+    }
+    int64_t q = warp_append(&A.counters[DM_CNT_CELLS], own);
+    if (own) {
+      if (q < A.cap_cells_out) {
+        reinterpret_cast<int4 *>(A.cells)[q] = make_int4(ip, tr.x, tr.y, tr.z);
+      } else {
+        flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// seed of escalated star k: the certified level-1 cell, else a global search
+__device__ __forceinline__ bool seed_of3(const DTArgs &A, const GridParams &g, int64_t k,
+                                         WarpL1<3> &Q1, int lane, int &ovf,
+                                         dmp::ExactScratch *W, int &ip, int3 &seed) {
+  int4 sd = A.esc_seed[k];
+  ip = sd.x & ~(1 << 30);
+  const bool certified = (sd.x >> 30) & 1;
+  seed = make_int3(-1, -1, -1);
+  if (certified) {
+    seed = make_int3(sd.y, sd.z, sd.w);
+  } else if (!gseed3(Q1, A, g, ip, lane, ovf, W, seed) &&
+             !gseed3_nn(A, g, ip, lane, ovf, W, seed)) {
+    seed = make_int3(-1, -1, -1);
+  }
+  return seed.x >= 0;
+}
+
 __global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
   __shared__ WarpL1<3> sm1[L2_WARPS];
+  __shared__ int scnt[L2_WARPS][4];
   dmp::ExactScratch WS;
   dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  WarpL2 &S = sm[w];
+  const StarStore S = {sm[w].tri, sm[w].open, scnt[w], L2_MAXTRI, L2_MAXOPEN};
   auto &Q1 = sm1[w];
   const GridParams g = *A.gp;
   const int64_t nesc = A.counters[DM_CNT_ESCALATED];
   for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
        k += (int64_t)gridDim.x * L2_WARPS) {
-    int4 sd = A.esc_seed[k];
-    const int ip = sd.x & ~(1 << 30);
-    const bool certified = (sd.x >> 30) & 1;
 #ifdef DM_L2_STATS
     long long t_start = clock64();
     if (lane < 8) g_l2w[blockIdx.x * L2_WARPS + w][lane] = 0;
     __syncwarp();
 #endif
-    int ovf = 0;
-    int3 seed = make_int3(-1, -1, -1);
-    if (certified) {
-      seed = make_int3(sd.y, sd.z, sd.w);
-    } else if (!gseed3(Q1, A, g, ip, lane, ovf, W, seed) &&
-               !gseed3_nn(A, g, ip, lane, ovf, W, seed)) {
-      seed = make_int3(-1, -1, -1);
-    }
-    if (seed.x < 0) {
+    int ovf = 0, ip;
+    int3 seed;
+    if (!seed_of3(A, g, k, Q1, lane, ovf, W, ip, seed)) {
       if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
       continue;
     }
-    if (lane == 0) {
-      S.ntri = 1;
-      S.tri[0] = seed;
-      S.open[0] = make_int3(seed.x, seed.y, seed.z);
-      S.open[1] = make_int3(seed.y, seed.z, seed.x);
-      S.open[2] = make_int3(seed.z, seed.x, seed.y);
-      S.nopen = 3;
-      S.flags = 0;
-    }
-    __syncwarp();
-    while (S.nopen > 0) {
-      int3 e = S.open[S.nopen - 1];
-      __syncwarp();
-      if (lane == 0) S.nopen--;
-      __syncwarp();
-      int u = e.x, v = e.y;
-      int y = gq3(A, g, ip, v, u, lane, ovf, W);
-      if (y < 0) continue;  // convex-hull face
-      if (S.ntri >= L2_MAXTRI) {
-        if (lane == 0) S.flags |= 1;
-        __syncwarp();
-        break;
-      }
-      if (lane == 0) S.tri[S.ntri++] = make_int3(v, u, y);
-      __syncwarp();
-      int es[2][3] = {{u, y, v}, {y, v, u}};
-      for (int q = 0; q < 2; ++q) {
-        int r = find_rev2(S, es[q][0], es[q][1], lane);
-        if (lane == 0) {
-          if (r >= 0) {
-            S.open[r] = S.open[S.nopen - 1];
-            S.nopen--;
-          } else if (S.nopen < L2_MAXOPEN) {
-            S.open[S.nopen++] = make_int3(es[q][0], es[q][1], es[q][2]);
-          } else {
-            S.flags |= 1;
-          }
-        }
-        __syncwarp();
-      }
-      if (S.flags) break;
-    }
-    if (S.flags && lane == 0) {
-      flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
-      A.counters[8] = ip;
-      A.counters[9] = S.ntri;
-      A.counters[10] = S.nopen;
-    }
+    const bool done = walk3(A, g, ip, seed, lane, ovf, W, S);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
     if (ip == A.dbg_vertex && A.dbg) {
-      // level-2 walk of the watched vertex: [1000] ntri, [1001] certified
-      // seed flag, [1002..1004] seed, [1008 + 3t ..] triangles in walk order
-      __syncwarp();
+      // level-2 walk of the watched vertex: [1000] ntri, [1002..1004] seed,
+      // [1008 + 3t ..] triangles in walk order
       if (lane == 0) {
-        A.dbg[1000] = S.ntri;
-        A.dbg[1001] = certified;
+        A.dbg[1000] = S.cnt[0];
         A.dbg[1002] = seed.x;
         A.dbg[1003] = seed.y;
         A.dbg[1004] = seed.z;
       }
-      for (int t = lane; t < S.ntri; t += 32) {
+      for (int t = lane; t < S.cnt[0]; t += 32) {
         A.dbg[1008 + 3 * t] = S.tri[t].x;
         A.dbg[1008 + 3 * t + 1] = S.tri[t].y;
         A.dbg[1008 + 3 * t + 2] = S.tri[t].z;
       }
       __syncwarp();
     }
-    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
 #ifdef DM_L2_STATS
-    __syncwarp();
     if (lane == 0 && k < kL2StatStars) {
       g_l2s[k][0] = clock64() - t_start;
-      g_l2s[k][1] = S.ntri | ((unsigned long long)ip << 32);
+      g_l2s[k][1] = S.cnt[0] | ((unsigned long long)ip << 32);
       for (int q = 1; q < 7; ++q) g_l2s[k][q + 1] = g_l2w[blockIdx.x * L2_WARPS + w][q];
     }
 #endif
-    for (int t0 = 0; t0 < S.ntri; t0 += 32) {
-      int t = t0 + lane;
-      bool own = false;
-      int3 tr = make_int3(0, 0, 0);
-      if (t < S.ntri) {
-        tr = S.tri[t];
-        own = ip < tr.x && ip < tr.y && ip < tr.z;
+    if (!done) {
+      // too large for shared memory: finished by level 3
+      if (lane == 0) {
+        int64_t k3 = atomicAdd((unsigned long long *)&A.counters[kCntL3], 1ull);
+        A.l3_list[k3] = (int32_t)k;
       }
-      int64_t q = warp_append(&A.counters[DM_CNT_CELLS], own);
-      if (own) {
-        if (q < A.cap_cells_out) {
-          reinterpret_cast<int4 *>(A.cells)[q] = make_int4(ip, tr.x, tr.y, tr.z);
-        } else {
-          flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
-        }
+      __syncwarp();
+      continue;
+    }
+    emit3(A, ip, S, lane);
+  }
+}
+
+__global__ void __launch_bounds__(32 * L3_WARPS) k_star3_l3(DTArgs A) {
+  __shared__ WarpL1<3> sm1[L3_WARPS];
+  dmp::ExactScratch WS;
+  dmp::ExactScratch *W = &WS;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gw = blockIdx.x * L3_WARPS + w;
+  const StarStore S = {A.l3_tri + (int64_t)gw * L3_CAP_TRI, A.l3_open + (int64_t)gw * L3_CAP_OPEN,
+                       A.l3_cnt + 4 * gw, L3_CAP_TRI, L3_CAP_OPEN};
+  const GridParams g = *A.gp;
+  const int64_t n3 = A.counters[kCntL3];
+  for (int64_t k3 = gw; k3 < n3; k3 += (int64_t)gridDim.x * L3_WARPS) {
+    const int64_t k = A.l3_list[k3];
+    int ovf = 0, ip;
+    int3 seed;
+    if (!seed_of3(A, g, k, sm1[w], lane, ovf, W, ip, seed)) {
+      if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
+      continue;
+    }
+    const bool done = walk3(A, g, ip, seed, lane, ovf, W, S);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    if (!done) {
+      if (lane == 0) {
+        flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+        A.counters[8] = ip;
+        A.counters[9] = S.cnt[0];
+        A.counters[10] = S.cnt[1];
+      }
+      __syncwarp();
+      continue;
+    }
+    emit3(A, ip, S, lane);
+  }
+}
+
+// linear walk of the star of ip (2D) from the link edge (a, b): forward
+// around p, then backward from a when a hull edge stops it
+__device__ __forceinline__ bool walk2(const DTArgs &A, const GridParams &g, int ip, int a, int b,
+                                      int lane, int &ovf, dmp::ExactScratch *W,
+                                      const StarStore &S) {
+  if (lane == 0) {
+    S.cnt[0] = 1;
+    S.tri[0] = make_int3(a, b, 0);
+    S.cnt[2] = 0;
+  }
+  __syncwarp();
+  bool hull = false;
+  int cur = b;
+  while (true) {
+    int nx = gq2(A, g, ip, cur, +1, lane, ovf, W);
+    if (nx < 0) {
+      hull = true;
+      break;
+    }
+    if (S.cnt[0] >= S.cap_tri) {
+      if (lane == 0) S.cnt[2] |= 1;
+      __syncwarp();
+      break;
+    }
+    if (lane == 0) S.tri[S.cnt[0]++] = make_int3(cur, nx, 0);
+    __syncwarp();
+    if (nx == a) break;  // closing triangle (p, cur, a)
+    cur = nx;
+  }
+  if (hull && !S.cnt[2]) {
+    cur = a;
+    while (true) {
+      int pv = gq2(A, g, ip, cur, -1, lane, ovf, W);
+      if (pv < 0) break;
+      if (S.cnt[0] >= S.cap_tri) {
+        if (lane == 0) S.cnt[2] |= 1;
+        __syncwarp();
+        break;
+      }
+      if (lane == 0) S.tri[S.cnt[0]++] = make_int3(pv, cur, 0);
+      __syncwarp();
+      cur = pv;
+    }
+  }
+  __syncwarp();
+  return S.cnt[2] == 0;
+}
+
+__device__ __forceinline__ void emit2(const DTArgs &A, int ip, const StarStore &S, int lane) {
+  const int ntri = S.cnt[0];
+  for (int t0 = 0; t0 < ntri; t0 += 32) {
+    int t = t0 + lane;
+    bool own = false;
+    int3 tr = make_int3(0, 0, 0);
+    if (t < ntri) {
+      tr = S.tri[t];
+      own = ip < tr.x && ip < tr.y;
+    }
+    int64_t q = warp_append(&A.counters[DM_CNT_CELLS], own);
+    if (own) {
+      if (q < A.cap_cells_out) {
+        A.cells[3 * q] = ip;
+        A.cells[3 * q + 1] = tr.x;
+        A.cells[3 * q + 2] = tr.y;
+      } else {
+        flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
       }
     }
-    __syncwarp();
   }
+  __syncwarp();
+}
+
+__device__ __forceinline__ bool seed_of2(const DTArgs &A, const GridParams &g, int64_t k,
+                                         WarpL1<2> &Q1, int lane, int &ovf,
+                                         dmp::ExactScratch *W, int &ip, int &a, int &b) {
+  int4 sd = A.esc_seed[k];
+  ip = sd.x & ~(1 << 30);
+  const bool certified = (sd.x >> 30) & 1;
+  a = -1;
+  b = -1;
+  if (certified) {
+    a = sd.y;
+    b = sd.z;
+  } else if (!gseed2(Q1, A, g, ip, lane, ovf, W, a, b) &&
+             !gseed2_nn(A, g, ip, lane, ovf, W, a, b)) {
+    a = -1;
+  }
+  return a >= 0;
 }
 
 __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
   __shared__ WarpL1<2> sm1[L2_WARPS];
+  __shared__ int scnt[L2_WARPS][4];
   dmp::ExactScratch WS;
   dmp::ExactScratch *W = &WS;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  WarpL2 &S = sm[w];
+  const StarStore S = {sm[w].tri, sm[w].open, scnt[w], L2_MAXTRI, L2_MAXOPEN};
   auto &Q1 = sm1[w];
   const GridParams g = *A.gp;
   const int64_t nesc = A.counters[DM_CNT_ESCALATED];
   for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
        k += (int64_t)gridDim.x * L2_WARPS) {
-    int4 sd = A.esc_seed[k];
-    const int ip = sd.x & ~(1 << 30);
-    const bool certified = (sd.x >> 30) & 1;
-    int ovf = 0;
-    int a = -1, b = -1;
-    if (certified) {
-      a = sd.y;
-      b = sd.z;
-    } else if (!gseed2(Q1, A, g, ip, lane, ovf, W, a, b) &&
-               !gseed2_nn(A, g, ip, lane, ovf, W, a, b)) {
-      a = -1;
-    }
-    if (a < 0) {
+    int ovf = 0, ip, a, b;
+    if (!seed_of2(A, g, k, Q1, lane, ovf, W, ip, a, b)) {
       if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
       continue;
     }
-    if (lane == 0) {
-      S.ntri = 1;
-      S.tri[0] = make_int3(a, b, 0);
-      S.flags = 0;
-    }
-    __syncwarp();
-    bool hull = false;
-    int cur = b;
-    while (true) {
-      int nx = gq2(A, g, ip, cur, +1, lane, ovf, W);
-      if (nx < 0) {
-        hull = true;
-        break;
-      }
-      if (S.ntri >= L2_MAXTRI) {
-        if (lane == 0) S.flags |= 1;
-        __syncwarp();
-        break;
-      }
-      if (nx == a) {
-        if (lane == 0) S.tri[S.ntri++] = make_int3(cur, nx, 0);
-        __syncwarp();
-        break;
-      }
-      if (S.ntri >= L2_MAXTRI) {
-        if (lane == 0) S.flags |= 1;
-        __syncwarp();
-        break;
-      }
-      if (lane == 0) S.tri[S.ntri++] = make_int3(cur, nx, 0);
-      __syncwarp();
-      cur = nx;
-    }
-    if (hull && !S.flags) {
-      cur = a;
-      while (true) {
-        int pv = gq2(A, g, ip, cur, -1, lane, ovf, W);
-        if (pv < 0) break;
-        if (S.ntri >= L2_MAXTRI) {
-          if (lane == 0) S.flags |= 1;
-          __syncwarp();
-          break;
-        }
-        if (lane == 0) S.tri[S.ntri++] = make_int3(pv, cur, 0);
-        __syncwarp();
-        cur = pv;
-      }
-    }
-    if (S.flags && lane == 0) {
-      flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
-      A.counters[8] = ip;
-      A.counters[9] = S.ntri;
-      A.counters[10] = S.nopen;
-    }
+    const bool done = walk2(A, g, ip, a, b, lane, ovf, W, S);
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
-    for (int t0 = 0; t0 < S.ntri; t0 += 32) {
-      int t = t0 + lane;
-      bool own = false;
-      int3 tr = make_int3(0, 0, 0);
-      if (t < S.ntri) {
-        tr = S.tri[t];
-        own = ip < tr.x && ip < tr.y;
+    if (!done) {
+      if (lane == 0) {
+        int64_t k3 = atomicAdd((unsigned long long *)&A.counters[kCntL3], 1ull);
+        A.l3_list[k3] = (int32_t)k;
       }
-      int64_t q = warp_append(&A.counters[DM_CNT_CELLS], own);
-      if (own) {
-        if (q < A.cap_cells_out) {
-          A.cells[3 * q] = ip;
-          A.cells[3 * q + 1] = tr.x;
-          A.cells[3 * q + 2] = tr.y;
-        } else {
-          flag_or(A.counters, DM_FLAG_CELL_OVERFLOW);
-        }
-      }
+      __syncwarp();
+      continue;
     }
-    __syncwarp();
+    emit2(A, ip, S, lane);
+  }
+}
+
+__global__ void __launch_bounds__(32 * L3_WARPS) k_star2_l3(DTArgs A) {
+  __shared__ WarpL1<2> sm1[L3_WARPS];
+  dmp::ExactScratch WS;
+  dmp::ExactScratch *W = &WS;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gw = blockIdx.x * L3_WARPS + w;
+  const StarStore S = {A.l3_tri + (int64_t)gw * L3_CAP_TRI, A.l3_open + (int64_t)gw * L3_CAP_OPEN,
+                       A.l3_cnt + 4 * gw, L3_CAP_TRI, L3_CAP_OPEN};
+  const GridParams g = *A.gp;
+  const int64_t n3 = A.counters[kCntL3];
+  for (int64_t k3 = gw; k3 < n3; k3 += (int64_t)gridDim.x * L3_WARPS) {
+    const int64_t k = A.l3_list[k3];
+    int ovf = 0, ip, a, b;
+    if (!seed_of2(A, g, k, sm1[w], lane, ovf, W, ip, a, b)) {
+      if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
+      continue;
+    }
+    const bool done = walk2(A, g, ip, a, b, lane, ovf, W, S);
+    if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    if (!done) {
+      if (lane == 0) {
+        flag_or(A.counters, DM_FLAG_STAR_OVERFLOW);
+        A.counters[8] = ip;
+        A.counters[9] = S.cnt[0];
+      }
+      __syncwarp();
+      continue;
+    }
+    emit2(A, ip, S, lane);
   }
 }
 
@@ -2577,14 +2707,17 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   DM_LAUNCH_CHECK();
   prof_mark(1, s);
   int g2 = kSMs * 8;
-  if (dim == 3)
+  if (dim == 3) {
     k_star3_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
-  else
+    k_star3_l3<<<L3_BLOCKS, 32 * L3_WARPS, 0, s>>>(a);
+  } else {
     k_star2_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
+    k_star2_l3<<<L3_BLOCKS, 32 * L3_WARPS, 0, s>>>(a);
+  }
   DM_LAUNCH_CHECK();
   prof_mark(2, s);
   if (g_prof_on && g_prof_n < kProfMax) ++g_prof_n;
-  note_launches(12);
+  note_launches(13);
   return DM_OK;
 }
 

@@ -325,6 +325,160 @@ __global__ void k_water_flag(const double *vp, int64_t n, int64_t row_len,
     if (vp[i] * scale < 1e-3 && i >= row_len) *flag = 1;
 }
 
+// ---------------------------------------------------------------------------
+// Gradient sizing (sizing/mesh_size_function.py:428-448):
+//   g = grad / (v + 0.10),  v = var / max(var) - min(var / max(var)),
+//   var = box_mean(vp^2) - box_mean(vp)^2
+// with the box means of scipy.ndimage.uniform_filter: separable, applied
+// axis by axis in order, window w per axis, origin 0 (covers i - w/2 ..
+// i - w/2 + w - 1) and 'reflect' boundaries (d c b a | a b c d | d c b a).
+// vp is read with the unit scale and water replacement of
+// dm_size_from_velocity.  Running sums in FP64, one thread per grid line.
+__device__ __forceinline__ int64_t reflect_index(int64_t j, int64_t L) {
+  const int64_t p = 2 * L;
+  j %= p;
+  if (j < 0) j += p;
+  return j < L ? j : p - 1 - j;
+}
+
+__global__ void k_box_mean_axis(const double *src_m, const double *src_s, double *dst_m,
+                                double *dst_s, int64_t nlines, int64_t L, int64_t st,
+                                int w, int first, double scale, double vp_water,
+                                int replace) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nlines;
+       l += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = (l / st) * (st * L) + (l % st);
+    auto val = [&](int64_t j, double &m, double &q) {
+      int64_t k = base + reflect_index(j, L) * st;
+      if (first) {
+        double v = src_m[k] * scale;
+        if (replace && v < 1e-3) v = vp_water;
+        m = v;
+        q = v * v;
+      } else {
+        m = src_m[k];
+        q = src_s[k];
+      }
+    };
+    const int64_t h = w / 2;
+    double sm = 0, sq = 0, a, b;
+    for (int64_t k = 0; k < w; ++k) {
+      val(k - h, a, b);
+      sm += a;
+      sq += b;
+    }
+    const double inv = 1.0 / w;
+    for (int64_t i = 0; i < L; ++i) {
+      dst_m[base + i * st] = sm * inv;
+      dst_s[base + i * st] = sq * inv;
+      if (i + 1 < L) {
+        double a1, b1, a0, b0;
+        val(i + 1 - h + w - 1, a1, b1);
+        val(i - h, a0, b0);
+        sm += a1 - a0;
+        sq += b1 - b0;
+      }
+    }
+  }
+}
+
+// var = s - m^2 into m; block maxima / minima of var into part
+__global__ void k_variance(double *m, const double *sq, int64_t n, double *part) {
+  double mx = -1e300, mn = 1e300;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = sq[i] - m[i] * m[i];
+    m[i] = v;
+    mx = fmax(mx, v);
+    mn = fmin(mn, v);
+  }
+  for (int o = 16; o; o >>= 1) {
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+  }
+  __shared__ double smx[8], smn[8];
+  if ((threadIdx.x & 31) == 0) {
+    smx[threadIdx.x >> 5] = mx;
+    smn[threadIdx.x >> 5] = mn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mx = smx[0];
+    mn = smn[0];
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+      mx = fmax(mx, smx[k]);
+      mn = fmin(mn, smn[k]);
+    }
+    part[2 * blockIdx.x] = mx;
+    part[2 * blockIdx.x + 1] = mn;
+  }
+}
+
+// g = grad / (var / max - min(var / max) + 0.1), in the order of the reference
+__global__ void k_gradient_term(const double *var, int64_t n, const double *part, int nb,
+                                double grad, double *g) {
+  double mx = -1e300, mn = 1e300;
+  for (int k = 0; k < nb; ++k) {
+    mx = fmax(mx, part[2 * k]);
+    mn = fmin(mn, part[2 * k + 1]);
+  }
+  const double lo = mn / mx;  // min of var / max (division is monotone for mx > 0)
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = var[i] / mx;
+    v -= lo;
+    g[i] = grad / (v + 0.10);
+  }
+}
+
+size_t gradient_term_workspace(int64_t n) {
+  Carve c(nullptr, 0);
+  c.take<double>(n);
+  c.take<double>(n);
+  c.take<double>(n);
+  c.take<double>(2 * 256);
+  return c.used + 256;
+}
+
+int gradient_term(const double *vp, const int32_t *dims, int dim, const int32_t *window,
+                  double scale, double vp_water, int replace, double grad, double *g,
+                  void *ws, size_t ws_bytes, cudaStream_t s) {
+  DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
+  DM_ARG_CHECK(dims && window, "dims / window");
+  int64_t n = 1;
+  for (int k = 0; k < dim; ++k) {
+    DM_ARG_CHECK(dims[k] > 0 && window[k] > 0, "dims and window must be positive");
+    n *= dims[k];
+  }
+  DM_ARG_CHECK(grad > 0, "grad must be > 0");
+  Carve c(ws, ws_bytes);
+  double *ms = c.take<double>(n), *ss = c.take<double>(n), *tm = c.take<double>(n);
+  double *part = c.take<double>(2 * 256);
+  if (!c.ok() || !ws) {
+    set_error("gradient_term: workspace %zu < required %zu", ws_bytes, c.used);
+    return DM_ERR_WORKSPACE;
+  }
+  // ping-pong: (g, ms) <-> (tm, ss); the output array g serves as a buffer
+  double *cur_m = nullptr, *cur_s = nullptr;
+  double *bufm[2] = {g, tm}, *bufs[2] = {ms, ss};
+  for (int axis = 0; axis < dim; ++axis) {
+    int64_t st = 1;
+    for (int k = axis + 1; k < dim; ++k) st *= dims[k];
+    const int64_t L = dims[axis], nlines = n / L;
+    double *om = bufm[axis & 1], *os = bufs[axis & 1];
+    k_box_mean_axis<<<grid_for(nlines, 128), 128, 0, s>>>(
+        axis == 0 ? vp : cur_m, cur_s, om, os, nlines, L, st, window[axis], axis == 0,
+        scale, vp_water, replace);
+    cur_m = om;
+    cur_s = os;
+  }
+  const int nb = 256;
+  k_variance<<<nb, 256, 0, s>>>(cur_m, cur_s, n, part);
+  k_gradient_term<<<grid_for(n, 256), 256, 0, s>>>(cur_m, n, part, nb, grad, g);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
 int size_from_velocity(double *vp, int64_t n, int64_t row_len,
                        const double *gterm, const SizeParams *sp_in,
                        double *cell, int *replaced_host, void *ws,

@@ -164,7 +164,25 @@ def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
         )
     gterm = None
     if sz_opts["grad"] > 0:
-        raise NotImplementedError("gradient-based sizing (grad > 0) has no device kernel yet")
+        # _gradient_sizing (sizing/mesh_size_function.py:428-448) on the device
+        print("Refining mesh sizes near sharp velocity gradients...")
+        st = sz_opts["stencil_size"]
+        window = [int(st)] * dim if np.isscalar(st) else [int(w) for w in st]
+        # water replacement as the reference decides it (any vp < 1e-3 in a
+        # row other than the first, sizing/mesh_size_function.py:154-165)
+        replace = bool(np.any(vp_host[1:] * scale < 1e-3))
+        vw = float(sz_opts["vp_water"]) if sz_opts["vp_water"] is not None else 0.0
+        if replace and (sz_opts["vp_water"] is None or vw < 1300 or vw > 1800):
+            raise ValueError("vp_water is None or out of bounds. It should be >1300 and <1800 m/s")
+        gterm = torch.empty_like(vpd)
+        gsz = N.c_sz(0)
+        N.call("dm_gradient_term_workspace_size", vpd.numel(), gsz)
+        gws = D.workspace(gsz.value)
+        N.call(
+            "dm_gradient_term", D.ptr(vpd), (N.c_int * 3)(*(list(shape) + [1] * (3 - dim))), dim,
+            (N.c_int * 3)(*(window + [1] * (3 - dim))), scale, vw, int(replace),
+            float(sz_opts["grad"]), D.ptr(gterm), D.ptr(gws), gws.numel(), D.stream_ptr(),
+        )
     if sz_opts["dt"] != 0.0 and sz_opts["cr_max"] != 0.0 and sz_opts["space_order"] != 0:
         if sz_opts["cr_max"] < 0:
             raise ValueError("Parameter `cr_max` must be > 0.0")
@@ -203,6 +221,30 @@ def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
     cell, vpd, bbox = _build_domain_pad(cell, vpd, bbox, sz_opts)
     fh = GridSizing.from_device(cell, bbox)
     return SizeFunction(bbox, fh, sz_opts["hmin"])
+
+
+def _gradient_sizing(vp, grad, stencil_size):
+    """Gradient sizing term of a velocity grid on the device (the reference's
+    _gradient_sizing, sizing/mesh_size_function.py:428-448): grad / (v + 0.1)
+    with v the normalised windowed variance of vp.  Returns 99999 for grad == 0."""
+    if grad == 0.0:
+        return 99999
+    if grad < 0:
+        raise ValueError("Parameter grad must be > 0")
+    vp = np.ascontiguousarray(np.asarray(vp, dtype=np.float64))
+    dim = vp.ndim
+    window = [int(stencil_size)] * dim if np.isscalar(stencil_size) else [int(w) for w in stencil_size]
+    vpd = torch.from_numpy(vp).to(D.device())
+    g = torch.empty_like(vpd)
+    gsz = N.c_sz(0)
+    N.call("dm_gradient_term_workspace_size", vpd.numel(), gsz)
+    ws = D.workspace(gsz.value)
+    N.call(
+        "dm_gradient_term", D.ptr(vpd), (N.c_int * 3)(*(list(vp.shape) + [1] * (3 - dim))), dim,
+        (N.c_int * 3)(*(window + [1] * (3 - dim))), 1.0, 0.0, 0, float(grad), D.ptr(g),
+        D.ptr(ws), ws.numel(), D.stream_ptr(),
+    )
+    return g.cpu().numpy()
 
 
 def _get_dimensions(shape, bbox):

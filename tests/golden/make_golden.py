@@ -179,5 +179,127 @@ def main():
     print(json.dumps(out, indent=1))
 
 
+def gradient_goldens():
+    """reference _gradient_sizing (sizing/mesh_size_function.py:428-448) and a
+    sizing pipeline with grad > 0"""
+    from SeismicMesh.sizing.mesh_size_function import _gradient_sizing
+
+    rng = np.random.default_rng(99)
+    out = {}
+    cases = {
+        "g2": ((15, 25), 10.0),
+        "g2w": ((9, 14), (40, 3)),  # windows larger than the grid
+        "g3": ((12, 9, 7), (3, 4, 5)),
+    }
+    for key, (shape, st) in cases.items():
+        vp = 1500 + 3000 * rng.random(shape)
+        vp[: shape[0] // 3] = 1500.0  # a flat layer: zero variance somewhere
+        out[key + "_vp"] = vp
+        out[key + "_stencil"] = np.atleast_1d(np.asarray(st, dtype=float))
+        out[key + "_out"] = _gradient_sizing(vp.copy(), 50.0, st)
+    vp2 = np.zeros((60, 90))
+    for i in range(60):
+        vp2[i] = 1500 + 3000 * i / 59
+    vp2 += rng.normal(0, 50, vp2.shape)
+    vp2[20:35, 30:60] = 4500.0  # a block of salt
+    bbox2 = (-6000.0, 0.0, 0.0, 18000.0)
+    xq2 = f32(np.column_stack([rng.uniform(-6000, 0, 3000), rng.uniform(0, 18000, 3000)]))
+    ef = SM.get_sizing_function_from_segy(None, bbox2, velocity_data=vp2.copy(), nz=60, nx=90,
+                                          hmin=75.0, wl=10, freq=2.0, grad=120.0, grade=0.15)
+    out.update(vp2=vp2, bbox2=np.asarray(bbox2), xq2=xq2, eval2=ef.eval(xq2))
+    save("gradient.npz", **out)
+
+
+def reference_test_goldens():
+    """the reference's mesh tests that read its own velocity fixtures and its
+    remaining SDF tests, re-run through the harness; only decoded velocity
+    arrays are stored (not the fixture files)"""
+    from SeismicMesh.sizing.mesh_size_function import read_velocity_model
+
+    tdir = os.path.join(ref_harness.REF, "tests")
+    # segyio (the reference's SEG-Y reader) is not installed: decode the SEG-Y
+    # rev 1 layout directly (3200-byte text and 400-byte binary headers,
+    # 240-byte trace headers, IBM float samples), traces as columns, then
+    # flipped like the reference's _read_segy
+    raw = open(os.path.join(tdir, "testing.segy"), "rb").read()
+    ns = int.from_bytes(raw[3220:3222], "big")
+    assert int.from_bytes(raw[3224:3226], "big") == 1  # IBM float samples
+    ntr = (len(raw) - 3600) // (240 + 4 * ns)
+    words = np.frombuffer(raw[3600:], ">u4").reshape(ntr, 60 + ns)[:, 60:].astype(np.uint64)
+    sign = 1.0 - 2.0 * ((words >> 31) & 1).astype(float)
+    expo = ((words >> 24) & 0x7F).astype(int) - 64
+    frac = (words & 0xFFFFFF).astype(float) / 2.0**24
+    vp2 = np.flipud((sign * frac * 16.0 ** expo).T)
+    nz2, nx2 = vp2.shape
+    vp3, nz3, nx3, ny3 = read_velocity_model(os.path.join(tdir, "test3D.bin"), nz=20, nx=10, ny=10,
+                                             byte_order="little", axes_order=(2, 0, 1),
+                                             axes_order_sort="F", dtype="float32")
+    save("velocity_fixtures.npz", segy_vp=np.asarray(vp2), bin_vp=np.asarray(vp3))
+    res = {}
+
+    def counts(p, t):
+        return [int(len(p)), int(len(t))]
+
+    # test_2dmesher_vs_water / test_2dmesher_r0m_values: water layer sizing
+    bbox = (-10000.0, 0.0, 0.0, 10000.0)
+    rect = SM.Rectangle(bbox)
+    vs = np.zeros((200, 200))
+    vs[0:150, :] = 1000
+    for hmin, key in ((10, "vs_water"), (75, "r0m")):
+        ef = SM.get_sizing_function_from_segy(None, bbox=bbox, grade=0.0, grad=0.0, wl=5, freq=2.0,
+                                              hmin=hmin, hmax=10e6, velocity_data=vs.copy(), nz=200, nx=200)
+        if key == "vs_water":
+            ef.hmin = None
+            p, t = SM.generate_mesh(rect, ef, h0=125, perform_checks=True, verbose=0)
+            res["vs_water"] = {"golden": [5616, 10955], "atol": 100, "harness": counts(p, t)}
+        else:
+            runs = []
+            for r0m, efh in ((False, 75), (True, 75), (True, 100)):
+                ef.hmin = efh
+                p, t = SM.generate_mesh(rect, ef, h0=125, perform_checks=True, r0m_is_h0=r0m, verbose=0)
+                runs.append(counts(p, t))
+            res["r0m"] = {"golden": [[15460, 30464], [10566, 20771], [8739, 17131]], "atol": 100,
+                          "harness": runs}
+    # test_2dmesher (testing.segy)
+    ef = SM.get_sizing_function_from_segy(None, bbox=bbox, grade=0.005, grad=50.0, wl=5, freq=5.0,
+                                          hmin=100, hmax=10e6, velocity_data=np.asarray(vp2).copy(),
+                                          nz=nz2, nx=nx2)
+    p, t = SM.generate_mesh(rect, ef, h0=100, perform_checks=True, verbose=0)
+    res["segy2d"] = {"golden": [7690, 15045], "atol": 100, "harness": counts(p, t)}
+    # test_2dmesher_domain_extension
+    ext = {}
+    for style, ans in (("linear_ramp", [9428, 18525]), ("edge", [9724, 19078]), ("constant", [9428, 18525])):
+        ef = SM.get_sizing_function_from_segy(None, bbox=bbox, grade=0.005, grad=50.0, stencil_size=100,
+                                              wl=5, freq=5.0, hmin=100, hmax=10e6, pad_style=style,
+                                              domain_pad=1e3, velocity_data=np.asarray(vp2).copy(),
+                                              nz=nz2, nx=nx2)
+        p, t = SM.generate_mesh(rect, ef, h0=100, perform_checks=True, verbose=0)
+        ext[style] = {"golden": ans, "harness": counts(p, t)}
+    res["domain_extension_2d"] = ext
+    # test_3dmesher (test3D.bin) and test_3dmesher_domain_extension
+    bbox3 = (-2e3, 0.0, 0.0, 1e3, 0.0, 1e3)
+    cube = SM.Cube(bbox3)
+    ef = SM.get_sizing_function_from_segy(None, bbox3, grade=0.005, grad=50, freq=2, wl=10, hmin=50,
+                                          nz=20, nx=10, ny=10, domain_pad=0.0,
+                                          velocity_data=np.asarray(vp3).copy())
+    p, t = SM.generate_mesh(domain=cube, edge_length=ef, h0=50, max_iter=25, perform_checks=False, verbose=0)
+    p, t = SM.sliver_removal(points=p, edge_length=ef, domain=cube, h0=50, verbose=0)
+    res["bin3d"] = {"golden": [16459, 89240], "atol": 100, "harness": counts(p, t)}
+    ext3 = {}
+    for style, ans in (("linear_ramp", [1388, 6592]), ("edge", [1383, 6545]), ("constant", [1406, 6622])):
+        ef = SM.get_sizing_function_from_segy(None, bbox3, grade=0.005, grad=150, freq=2, wl=5, hmin=150,
+                                              nz=20, nx=10, ny=10, domain_pad=200, pad_style=style,
+                                              velocity_data=np.asarray(vp3).copy())
+        p, t = SM.generate_mesh(domain=cube, edge_length=ef, h0=150, perform_checks=False, verbose=0)
+        p, t = SM.sliver_removal(points=p, domain=cube, edge_length=ef, h0=150, verbose=0)
+        ext3[style] = {"golden": ans, "harness": counts(p, t)}
+    res["domain_extension_3d"] = ext3
+    with open(os.path.join(HERE, "reference_tests2.json"), "w") as fh:
+        json.dump(res, fh, indent=1)
+    print(json.dumps(res, indent=1))
+
+
 if __name__ == "__main__":
-    main()
+    parts = sys.argv[1:] or ["main"]
+    for part in parts:
+        {"main": main, "gradient": gradient_goldens, "reftests2": reference_test_goldens}[part]()

@@ -251,3 +251,19 @@ def test_device_predicates_match_host_exact_predicates(cuda):
     assert f(Pd.data_ptr(), Tn.data_ptr(), int(nz.sum()), 1, out.data_ptr(), None) == 0
     np.testing.assert_array_equal(out.cpu().numpy(), s_host)
     assert (o_host == 0).sum() > 50  # exact degeneracies were exercised
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,m", [(3, 600), (2, 400)])
+def test_very_large_star_is_completed(cuda, dim, m):
+    """A vertex whose star outgrows the shared-memory star (192 link
+    triangles) is finished by the level-3 kernel; the triangulation is Qhull's."""
+    rng = np.random.default_rng(31 + dim)
+    s = rng.standard_normal((m, dim))
+    p = np.vstack([np.zeros(dim), s / np.linalg.norm(s, axis=1)[:, None]])
+    p = p.astype(np.float32).astype(np.float64)
+    eng = _Engine(dim, p, 0, grid=False)
+    nc = eng.triangulate()
+    cells = eng.cells[:nc].cpu().numpy()
+    assert (cells == 0).any(1).sum() >= m
+    dc.assert_same_triangulation(p, cells)

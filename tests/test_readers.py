@@ -1,0 +1,60 @@
+"""Velocity model readers (sizing/mesh_size_function.py:590-646) on files
+written here: a SEG-Y rev 1 file with IBM float samples holding the decoded
+reference fixture, and raw binaries in both byte orders and axis orders."""
+import numpy as np
+
+from seismicmesh_gb300.sizing.mesh_size_function import _read_bin, _read_segy
+
+from conftest import golden
+
+
+def _to_ibm(v):
+    """float64 -> IBM System/360 single (sign, base-16 exponent + 64, 24-bit
+    fraction), truncating like the hardware format"""
+    out = np.zeros(v.shape, dtype=np.uint32)
+    for idx, x in np.ndenumerate(v):
+        if x == 0:
+            continue
+        s = 0x80000000 if x < 0 else 0
+        a = abs(float(x))
+        e = 64
+        while a >= 1.0:
+            a /= 16.0
+            e += 1
+        while a < 1.0 / 16.0:
+            a *= 16.0
+            e -= 1
+        out[idx] = s | (e << 24) | int(a * (1 << 24))
+    return out
+
+
+def test_segy_reader_roundtrip(tmp_path):
+    vp = golden("velocity_fixtures.npz")["segy_vp"]
+    nz, nx = vp.shape
+    traces = np.flipud(vp).T  # trace k = column k before the flip
+    words = _to_ibm(traces)
+    hdr = bytearray(3600)
+    hdr[3220:3222] = int(nz).to_bytes(2, "big")
+    hdr[3224:3226] = (1).to_bytes(2, "big")
+    body = b"".join(bytes(240) + words[k].astype(">u4").tobytes() for k in range(nx))
+    f = tmp_path / "m.segy"
+    f.write_bytes(bytes(hdr) + body)
+    got, gnz, gnx, gny = _read_segy(str(f))
+    assert (gnz, gnx, gny) == (nz, nx, 0)
+    np.testing.assert_array_equal(got, vp)
+
+
+def test_binary_reader_orders(tmp_path):
+    rng = np.random.default_rng(3)
+    nz, nx, ny = 5, 4, 3
+    for order in ((0, 1, 2), (2, 0, 1), (1, 2, 0)):
+        for bo, code in (("little", "<f4"), ("big", ">f4")):
+            for sort in ("F", "C"):
+                axes = [nz, nx, ny]
+                stored = [axes[o] for o in np.argsort(order)]
+                data = rng.random(stored).astype(np.float32)
+                f = tmp_path / f"m_{bo}_{sort}.bin"
+                data.reshape(-1, order=sort).astype(code).tofile(str(f))
+                got, *_ = _read_bin(str(f), nz, nx, ny, bo, order, sort, "float32")
+                want = np.flipud(data.transpose(order))
+                np.testing.assert_array_equal(got, want)
