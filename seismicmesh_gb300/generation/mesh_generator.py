@@ -137,6 +137,30 @@ def snap_to_grid(p, e):
     return np.rint(np.asarray(p, dtype=float) / q) * q
 
 
+def _fd_gradients(fd, p, d, deps):
+    """one-sided finite-difference gradient of a host SDF and its squared
+    norm floored at deps (generation/mesh_generator.py:773-780)"""
+    dim = p.shape[1]
+    grads = []
+    for i in range(dim):
+        q = p.copy()
+        q[:, i] += deps
+        grads.append((fd(q) - d) / deps)
+    g2 = sum(g**2 for g in grads)
+    return np.vstack(grads), np.where(g2 < deps, deps, g2)
+
+
+def _project_points_back_host(p, fd, deps, hmin, idx):
+    """_project_points_back_newton (generation/mesh_generator.py:762-784) for
+    host-callable domains: one Newton step for points outside level idx"""
+    d = fd(p)
+    ix = d > 0.0 if idx == 0 else np.logical_and(d > 0.0, d < hmin / 1.5)
+    if ix.any():
+        g, g2 = _fd_gradients(fd, p[ix], d[ix], deps)
+        p[ix] -= (d[ix] * g / g2).T
+    return p
+
+
 class _Engine:
     """Device state of one meshing run.  With grid=True the points live on the
     position grid of the run (snapped here, kept there by the update
@@ -324,8 +348,33 @@ class _Engine:
         self.counters[N.CNT_KEPT] = nk
         return nk
 
+    def project_host(self, levels, deps, hmin):
+        """Newton projection on the host, for runs with a host-callable level
+        (the slow path: positions make one round trip per iteration)"""
+        p = D.from_points(self.P, self.dim)
+        for idx, lv in enumerate(levels):
+            p = _project_points_back_host(p, lv, deps, hmin, idx)
+        if self.grid_exp != N.DM_NO_GRID:
+            p = snap_to_grid(p, self.grid_exp)
+        self.P.copy_(D.to_points(p, self.dim))
+
     def improve_level_set(self, domain, deps):
         if not domain.is_program:
+            # _improve_level_set_newton (generation/mesh_generator.py:741-759)
+            # with the host callable
+            bid = self.boundary_vertices(N.CNT_KEPT).long().cpu().numpy()
+            if len(bid) == 0:
+                return
+            p = D.from_points(self.P, self.dim)
+            alpha = 1.0
+            for it in range(5):
+                d = domain(p[bid])
+                g, g2 = _fd_gradients(domain, p[bid], d, deps)
+                p[bid] -= alpha * (d * g / g2).T
+                alpha /= it + 1
+            if self.grid_exp != N.DM_NO_GRID:
+                p = snap_to_grid(p, self.grid_exp)
+            self.P.copy_(D.to_points(p, self.dim))
             return
         bid = self.boundary_vertices(N.CNT_KEPT)
         if bid.numel():
@@ -458,12 +507,10 @@ def generate_mesh(domain, edge_length, comm=None, **kwargs):  # noqa: C901
         for sub in gen_opts["subdomains"]:
             sfd, _, _ = _unpack_domain(sub, gen_opts)
             levels.append(sfd)
-    for lv in levels:
-        if not lv.is_program:
-            raise NotImplementedError(
-                "a host-callable domain cannot drive the device Newton projection; "
-                "pass a geometry object (Disk, Rectangle, Ball, Cube, ..., Union, ...)"
-            )
+    # a host-callable level moves the projection to the host (slow path)
+    host_levels = not all(lv.is_program for lv in levels)
+    if host_levels:
+        print_msg1("Host-callable domain: the Newton projection runs on the host")
 
     eng = _Engine(dim, p, nfix)
     count = 0
@@ -476,7 +523,9 @@ def generate_mesh(domain, edge_length, comm=None, **kwargs):  # noqa: C901
             _termination(eng, fd, gen_opts, h0, deps)
             break
         eng.build_adjacency()
-        eng.step(sizing, levels, L0mult, delta_t, h0, deps)
+        eng.step(sizing, [] if host_levels else levels, L0mult, delta_t, h0, deps)
+        if host_levels:
+            eng.project_host(levels, deps, h0)
         maxdp = eng.max_movement(delta_t)
         print_msg2(
             "Iteration #%d, max movement is %f, there are %d vertices and %d cells"
