@@ -223,6 +223,7 @@ def run_ours(args, world, rank, local):
     sticky = torch.zeros(1, dtype=torch.int64, device="cuda")
 
     def iteration_async():
+        stream = D.stream_ptr()  # the current stream (a capture stream inside a graph)
         N.call("dm_delaunay", 3, D.ptr(eng.P), eng.n, D.ptr(eng.cells), eng.cap_cells,
                D.ptr(eng.counters), D.ptr(eng.ws_dt), eng.ws_dt.numel(), stream)
         N.call("dm_filter_cells", 3, D.ptr(eng.P), D.ptr(eng.cells), eng.cap_cells, prog,
@@ -244,30 +245,68 @@ def run_ours(args, world, rank, local):
         eng.build_adjacency()
         eng.step(sizing, levels, L0mult, 0.30, H, deps)
     torch.cuda.synchronize()
+    # one DistMesh iteration as a CUDA graph: positions are copied back in
+    # place so every replay sees the same buffers.  Captured with the star
+    # kernels' event marks as event-record nodes (timed at every replay).
+    graph = None
+    try:
+        def iteration_inplace():
+            iteration_async()
+            eng.P, eng.P2 = eng.P2, eng.P
+            eng.P.copy_(eng.P2)
+
+        s0 = torch.cuda.Stream()
+        s0.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s0):
+            iteration_inplace()  # warm the capture stream
+        torch.cuda.current_stream().wait_stream(s0)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        L.dmprof_enable(1)  # the captured marks are entry 0 of the event table
+        launches_c0 = L.dmprof_launches()
+        with torch.cuda.graph(graph):
+            iteration_inplace()
+        launches_per_step = L.dmprof_launches() - launches_c0
+    except Exception as exc:  # plain stream launches if capture is not possible
+        print(f"CUDA graph capture failed ({exc}); timing stream launches", file=sys.stderr)
+        graph = None
+    torch.cuda.synchronize()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = L.dmprof_launches()
-    L.dmprof_enable(1)
     barrier(world)
     torch.cuda.synchronize()
+    l1_total = l2_total = 0.0
+    l_calls = 0
+    ms1, ms2, calls = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
             flush.fill_(float(k))
+            if graph is None:
+                L.dmprof_enable(1)
             ev[k][0].record()
-            iteration_async()
+            if graph is not None:
+                graph.replay()
+            else:
+                iteration_async()
             ev[k][1].record()
+            # star-kernel times of this step (outside the step's events)
+            torch.cuda.synchronize()
+            L.dmprof_read(ms1, ms2, calls)
+            l1_total += ms1.value
+            l2_total += ms2.value
+            l_calls += calls.value
         torch.cuda.synchronize()
-    barrier(world)
     L.dmprof_enable(0)
-    launches = L.dmprof_launches() - launches0
+    barrier(world)
+    launches = (launches_per_step * args.steps if graph is not None
+                else L.dmprof_launches() - launches0)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
     c = eng.counters_host()
     flags = int(sticky.item())
     if flags:
         raise RuntimeError(f"device flags {flags:#x} during the timed iterations")
-    ms1, ms2, calls = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
-    L.dmprof_read(ms1, ms2, calls)
     n_cells = int(c[N.CNT_CELLS])
     max_ms = reduce_max(total_ms, world, "nccl")
     value = world * n * args.steps / (max_ms / 1000.0)
@@ -276,8 +315,8 @@ def run_ours(args, world, rank, local):
     # algorithmic bytes per launch = points read (16 B each) + cells written
     # (16 B each) + candidate grid reads (4 B per point for the sorted ids and
     # 8 B per cell range), i.e. 16 n + 16 T + 4 n + 8 n_cells_grid ~ 16 T + 28 n
-    l1_ms = ms1.value / max(calls.value, 1)
-    l2_ms = ms2.value / max(calls.value, 1)
+    l1_ms = l1_total / max(l_calls, 1)
+    l2_ms = l2_total / max(l_calls, 1)
     alg_bytes = 16 * n_cells + 28 * n
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (l1_ms / 1000.0) / 1e9
@@ -329,7 +368,7 @@ def run_ours(args, world, rank, local):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32 (positions, forces); exact f64 expansions in the predicates",
+            "dtype": "f32 (positions on a 2^-24-relative grid, forces); exact 64/128/192-bit integer predicates",
             "data": "synthetic (initial lattice of the unit ball, seeded decimation)",
             "config": {
                 "workload": "3D unit ball, h=0.02, DistMesh iterations after 'warmup' iterations from the initial lattice",
@@ -346,7 +385,7 @@ def run_ours(args, world, rank, local):
                 "peak_kind": peak_kind,
                 "unit": "GB/s",
                 "frac": achieved / peak,
-                "traffic": None,
+                "traffic": measured_traffic(),
                 "alg_bytes_per_launch": alg_bytes,
                 "avg_launch_ms": l1_ms,
                 "level2_ms": l2_ms,
@@ -360,6 +399,47 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+PROFILE_L1 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                          "k_star3_l1_ball_h002.md")
+
+
+def measured_traffic():
+    """DRAM bytes (read + write) per k_star3_l1 launch from the committed ncu
+    summary of this workload (the line 'dram_bytes_per_launch: N'), or None"""
+    try:
+        for line in open(PROFILE_L1):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return int(line.split(":")[1].strip().replace(",", ""))
+    except OSError:
+        pass
+    return None
+
+
+def ncu_case(args):
+    """the bench workload (3D unit ball, h = 0.02) for args.warmup iterations,
+    then one more triangulation: the launch an ncu capture selects"""
+    import torch
+
+    import seismicmesh_gb300 as sm
+    from seismicmesh_gb300.generation import mesh_generator as MG
+
+    ball = sm.Ball([0.0, 0.0, 0.0], 1.0)
+    fd = MG._Domain(ball)
+    sizing = MG._Sizing(H, 3)
+    opts = {"points": None, "r0m_is_h0": False, "seed": 0}
+    p0 = MG._initialize_points(3, 0.1 * H, np.array([[-1.0, 1.0]] * 3), sizing, fd, H, opts, np.empty((0, 3)))
+    eng = MG._Engine(3, p0, 0)
+    deps = float(np.sqrt(np.finfo(float).eps) * H)
+    for _ in range(args.warmup):
+        eng.triangulate()
+        eng.filter(fd, 0.1 * H)
+        eng.build_adjacency()
+        eng.step(sizing, [fd], 1 + 0.4 / 2**2, 0.30, H, deps)
+    eng.triangulate()
+    torch.cuda.synchronize()
+    print("ncu case done:", eng.n, "points", int(eng.counters_host()[0]), "cells")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -368,7 +448,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="profiling case: the bench workload for --warmup iterations, then one "
+                         "triangulation (no timing, no JSON line)")
     args = ap.parse_args()
+    if args.ncu_case:
+        ncu_case(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     world, rank, local = dist_init()

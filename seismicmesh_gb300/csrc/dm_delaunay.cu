@@ -2629,7 +2629,14 @@ static void prof_mark(int slot, cudaStream_t s) {
   if (!g_prof_on || g_prof_n >= kProfMax) return;
   cudaEvent_t &e = g_prof_ev[g_prof_n][slot];
   if (!e) cudaEventCreate(&e);
-  cudaEventRecord(e, s);
+  // inside a stream capture the mark becomes an event-record node of the
+  // graph, re-recorded (with its timestamp) at every replay
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &st);
+  if (st == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+  else
+    cudaEventRecord(e, s);
 }
 
 int delaunay_workspace(int dim, int64_t n, size_t *bytes) {
