@@ -377,6 +377,13 @@ struct L1<2> {
 };
 
 constexpr int L1_WARPS = 4;
+// minimum resident blocks per SM requested from the register allocator
+#ifndef DM_L1_MINB
+#define DM_L1_MINB 1
+#endif
+#ifndef DM_L2_MINB
+#define DM_L2_MINB 5  // 96 registers: 5 blocks per SM measured 2-8 % faster than 4
+#endif
 
 template <int DIM>
 struct WarpL1 {
@@ -418,12 +425,11 @@ __device__ __forceinline__ int o3L_exact(const WarpL1<3> &S, const float *P, int
                                          int a, int b, int c, dmp::ExactScratch *W) {
   const int4 IA = S.ci[a], IB = S.ci[b], IC = S.ci[c];
   if (IA.w & IB.w & IC.w) return dmp::orient3_fx(IA, IB, IC);
-  float pr[3], ar[3], br[3], cr[3];
-  load_pt<3>(P, ip, pr);
-  load_pt<3>(P, S.id[a], ar);
-  load_pt<3>(P, S.id[b], br);
-  load_pt<3>(P, S.id[c], cr);
-  return dmp::orient3_slow(pr, ar, br, cr, W);
+  load_pt<3>(P, ip, W->pt[0]);
+  load_pt<3>(P, S.id[a], W->pt[1]);
+  load_pt<3>(P, S.id[b], W->pt[2]);
+  load_pt<3>(P, S.id[c], W->pt[3]);
+  return dmp::orient3_slow(W->pt[0], W->pt[1], W->pt[2], W->pt[3], W);
 }
 
 __device__ __forceinline__ int o3L(const WarpL1<3> &S, const float *P, int ip,
@@ -495,20 +501,27 @@ __device__ __forceinline__ int is3L_exact(const WarpL1<3> &S, const float *P, in
                                           dmp::ExactScratch *W) {
   const int4 IA = S.ci[a], IB = S.ci[b], IC = S.ci[c], ID = S.ci[d];
   if (IA.w & IB.w & IC.w & ID.w) return dmp::insph3_fx_sos(IA, IB, IC, ID);
-  float pr[3], ar[3], br[3], cr[3], dr[3];
-  load_pt<3>(P, ip, pr);
-  load_pt<3>(P, S.id[a], ar);
-  load_pt<3>(P, S.id[b], br);
-  load_pt<3>(P, S.id[c], cr);
-  load_pt<3>(P, S.id[d], dr);
-  return insph3_sos(pr, ar, br, cr, dr, &ovf, W);
+  float(*pt)[3] = W->pt;
+  load_pt<3>(P, ip, pt[0]);
+  load_pt<3>(P, S.id[a], pt[1]);
+  load_pt<3>(P, S.id[b], pt[2]);
+  load_pt<3>(P, S.id[c], pt[3]);
+  load_pt<3>(P, S.id[d], pt[4]);
+  int s = dmp::insph3_slow(pt[0], pt[1], pt[2], pt[3], pt[4], &ovf, W);
+  return s ? s : dmp::insph3_sos_tail(pt[0], pt[1], pt[2], pt[3], pt[4], W);
 }
 
 // gift-wrap query on face (p, a, b): winner among candidates y with
 // orient3(p,a,b,y) > 0 whose sphere through the face is smallest; -1 if none.
-__device__ __forceinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
-                                    int a, int b, int lane, int &ovf,
-                                    dmp::ExactScratch *W) {
+// out of line: one copy serves the seed search and the walk (instruction
+// cache); it owns no arrays (exact-stage temporaries live in W)
+#ifdef DM_GW3L_INLINE
+static __device__ __forceinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
+#else
+static __device__ __noinline__ int gw3L(const WarpL1<3> &S, const float *P, int ip,
+#endif
+                                        int a, int b, int lane, int &ovf,
+                                        dmp::ExactScratch *W) {
   const int nc = S.nc;
   float4 A = S.c[a], B = S.c[b];
   float nx = A.y * B.z - A.z * B.y, ny = A.z * B.x - A.x * B.z,
@@ -1028,7 +1041,7 @@ __device__ __forceinline__ void escalate(const DTArgs &A, int p, int4 seed,
   }
 }
 
-__global__ void __launch_bounds__(32 * L1_WARPS) k_star3_l1(DTArgs A) {
+__global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A) {
   __shared__ WarpL1<3> sm[L1_WARPS];
   dmp::ExactScratch WS;
   dmp::ExactScratch *W = &WS;
@@ -2362,7 +2375,7 @@ __device__ __forceinline__ bool seed_of3(const DTArgs &A, const GridParams &g, i
   return seed.x >= 0;
 }
 
-__global__ void __launch_bounds__(32 * L2_WARPS) k_star3_l2(DTArgs A) {
+__global__ void __launch_bounds__(32 * L2_WARPS, DM_L2_MINB) k_star3_l2(DTArgs A) {
   __shared__ WarpL2 sm[L2_WARPS];
   __shared__ WarpL1<3> sm1[L2_WARPS];
   __shared__ int scnt[L2_WARPS][4];

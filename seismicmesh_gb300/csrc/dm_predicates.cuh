@@ -252,6 +252,7 @@ struct ExactScratch {
   double e2[2];
   double d3tmp[20];
   double dx[4][3];  // exact differences of the FP64 filter stages
+  float pt[5][3];   // raw points handed to the exact stages by the star kernels
 };
 
 // orient3(a,b,c,d) = det3(b,c,d) - det3(a,c,d) + det3(a,b,d) - det3(a,b,c)
