@@ -327,6 +327,31 @@ int dm_compact_vertices(int32_t dim, const float *points, float *points_out,
                         size_t workspace_bytes, void *stream);
 /* simp_vol / simp_qual (geometry/utils.py:175-201, 252-274); either output
  * may be NULL.  Float64 outputs computed from the FP32 points. */
+/* calc_re_ratios (geometry/utils.py:17-54): circumradius / shortest edge of
+ * each of the nc cells, the radius-edge ratio quality metric; points
+ * double[n][dim] on the device, arithmetic in FP64. */
+int dm_radius_edge_ratios(int32_t dim, const double *points, const int32_t *cells,
+                          int64_t nc, double *ratios, void *stream);
+/* Cell quality of the reference's benchmark reports (benchmarks/helpers.py
+ * print_stats_2d/3d): quality = dim * inradius / circumradius and, in 3D,
+ * the minimum sine of the six dihedral angles divided by the regular
+ * tetrahedron's (2 sqrt(2) / 3).  points double[n][dim] on the device;
+ * min_sin_dihedral may be NULL (always unused in 2D).  FP64. */
+int dm_cell_quality(int32_t dim, const double *points, const int32_t *cells, int64_t nc,
+                    double *quality, double *min_sin_dihedral, void *stream);
+/* do_any_overlap (geometry/utils.py:745-817): points double[n][dim] and
+ * cells int32[nc][dim+1] on the device.  The centroid of every cell is tested
+ * against every other cell sharing a vertex with it, in FP64 with the
+ * reference's operation order (barycentric coordinates in 2D,
+ * calc_4x4determinant signs in 3D, fast_geometry.cpp:482-495).  pairs
+ * int32[cap][2] receives (cell, other cell) once per shared vertex, ordered
+ * by cell, vertex slot, other cell; *n_pairs (host) is the count.  Blocks
+ * the calling thread on the stream.  DM_ERR_CAPACITY, with *n_pairs set,
+ * when cap is too small; DM_ERR_ARG for a vertex index outside [0, n). */
+int dm_overlap_workspace_size(int32_t dim, int64_t n, int64_t nc, size_t *bytes);
+int dm_overlap_pairs(int32_t dim, const double *points, int64_t n, const int32_t *cells,
+                     int64_t nc, int32_t *pairs, int64_t cap, int64_t *n_pairs,
+                     void *workspace, size_t workspace_bytes, void *stream);
 int dm_simplex_metrics(int32_t dim, const float *points, const int32_t *cells,
                        int64_t nc, double *volume, double *quality,
                        void *stream);

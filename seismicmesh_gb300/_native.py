@@ -80,6 +80,13 @@ SIGNATURES = {
     ),
     "dm_cell_centroids": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
     "dm_adjacency_workspace_size": (c_int, [c_int, c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_radius_edge_ratios": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p]),
+    "dm_cell_quality": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
+    "dm_overlap_workspace_size": (c_int, [c_int, c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_overlap_pairs": (
+        c_int,
+        [c_int, c_p, c_i64, c_p, c_i64, c_p, c_i64, ctypes.POINTER(c_i64), c_p, c_sz, c_p],
+    ),
     "dm_gradient_term_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
     "dm_gradient_term": (
         c_int,

@@ -68,6 +68,14 @@ int compact_vertices(int dim, const float *P, float *Pout, int64_t n,
                      int32_t *cells, int64_t cap, int count_index,
                      int64_t *counters, int64_t *n_out, void *ws,
                      size_t ws_bytes, cudaStream_t s);
+int re_ratios(int dim, const double *P, const int32_t *cells, int64_t nc, double *out,
+              cudaStream_t s);
+size_t overlap_workspace(int dim, int64_t n, int64_t nc);
+int cell_quality(int dim, const double *X, const int32_t *cells, int64_t nc, double *quality,
+                 double *min_sin, cudaStream_t s);
+int overlap_pairs(int dim, const double *X, int64_t n, const int32_t *cells, int64_t nc,
+                  int32_t *pairs, int64_t cap, int64_t *n_pairs, void *ws, size_t ws_bytes,
+                  cudaStream_t s);
 int simplex_metrics(int dim, const float *P, const int32_t *cells, int64_t nc,
                     double *vol, double *qual, cudaStream_t s);
 size_t laplacian_workspace(int64_t n);
@@ -94,7 +102,7 @@ extern "C" {
 
 int dm_version(void) { return 10000; }
 const char *dm_last_error(void) { return dm::last_error(); }
-int dm_abi_count(void) { return 41; }
+int dm_abi_count(void) { return 45; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
   dmp::ExactScratch W;
@@ -299,6 +307,25 @@ int dm_compact_vertices(int32_t dim, const float *points, float *points_out,
   return dm::compact_vertices(dim, points, points_out, n, cells, cap_cells,
                               count_index, counters, n_out_host, workspace,
                               workspace_bytes, S(stream));
+}
+int dm_radius_edge_ratios(int32_t dim, const double *points, const int32_t *cells,
+                          int64_t nc, double *ratios, void *stream) {
+  return dm::re_ratios(dim, points, cells, nc, ratios, S(stream));
+}
+int dm_cell_quality(int32_t dim, const double *points, const int32_t *cells, int64_t nc,
+                    double *quality, double *min_sin_dihedral, void *stream) {
+  return dm::cell_quality(dim, points, cells, nc, quality, min_sin_dihedral, S(stream));
+}
+int dm_overlap_workspace_size(int32_t dim, int64_t n, int64_t nc, size_t *bytes) {
+  DM_ARG_CHECK(bytes && n >= 0 && nc >= 0, "arguments");
+  *bytes = dm::overlap_workspace(dim, n, nc);
+  return DM_OK;
+}
+int dm_overlap_pairs(int32_t dim, const double *points, int64_t n, const int32_t *cells,
+                     int64_t nc, int32_t *pairs, int64_t cap, int64_t *n_pairs,
+                     void *workspace, size_t workspace_bytes, void *stream) {
+  return dm::overlap_pairs(dim, points, n, cells, nc, pairs, cap, n_pairs, workspace,
+                           workspace_bytes, S(stream));
 }
 int dm_simplex_metrics(int32_t dim, const float *points, const int32_t *cells,
                        int64_t nc, double *volume, double *quality,

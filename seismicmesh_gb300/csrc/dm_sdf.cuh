@@ -39,6 +39,7 @@ enum SdfXform : int32_t {
   XF_RY = 4,
   XF_RZ = 8,
   XF_STRETCH = 16,
+  XF_REPEAT = 32,  // periodic repetition, applied before the other transforms
 };
 constexpr int SDF_OPREC = 4;  // {op, param offset, child count, xform flags}
 constexpr int SDF_STACK = 16;
@@ -257,6 +258,15 @@ __device__ __forceinline__ Dual eval_primitive(int op, const float *pp,
   const float *t = pp + prim_nparams<DIM>(op);
   const float *T = nullptr, *RX = nullptr, *RY = nullptr, *RZ = nullptr,
               *SV = nullptr;
+  if (xf & XF_REPEAT) {
+    // Repeat (geometry/signed_distance_functions.py:283-297):
+    // q = mod(x + p/2, p) - p/2 with a floor-based mod (numpy's np.mod)
+    for (int k = 0; k < DIM; ++k) {
+      const float p = t[k], y = q[k] + 0.5f * p;
+      q[k] = y - p * floorf(y / p) - 0.5f * p;
+    }
+    t += DIM;
+  }
   if (xf & XF_TRANSLATE) {
     T = t;
     t += DIM;

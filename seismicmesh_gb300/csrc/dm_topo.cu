@@ -281,6 +281,70 @@ __global__ void k_simplex_metrics(const float *P, const int32_t *cells,
   }
 }
 
+// calc_re_ratios (geometry/utils.py:17-54): circumradius / shortest edge of
+// each simplex, in FP64 (circumcentre from the normal equations of the edge
+// vectors relative to the first vertex)
+template <int DIM>
+__global__ void k_re_ratios(const double *X, const int32_t *cells, int64_t nc, double *out) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    double x[4][3] = {};
+    for (int k = 0; k <= DIM; ++k) {
+      const int64_t v = cells[(DIM + 1) * c + k];
+      for (int d = 0; d < DIM; ++d) x[k][d] = X[v * DIM + d];
+    }
+    double minl2 = 1e300;
+    for (int i = 0; i <= DIM; ++i)
+      for (int j = i + 1; j <= DIM; ++j) {
+        double l2 = 0;
+        for (int k = 0; k < DIM; ++k) l2 += (x[i][k] - x[j][k]) * (x[i][k] - x[j][k]);
+        minl2 = fmin(minl2, l2);
+      }
+    double r2;
+    if (DIM == 2) {
+      double a0 = x[1][0] - x[0][0], a1 = x[1][1] - x[0][1];
+      double b0 = x[2][0] - x[0][0], b1 = x[2][1] - x[0][1];
+      double d = 2 * (a0 * b1 - a1 * b0);
+      double la = a0 * a0 + a1 * a1, lb = b0 * b0 + b1 * b1;
+      double ux = (b1 * la - a1 * lb) / d, uy = (a0 * lb - b0 * la) / d;
+      r2 = ux * ux + uy * uy;
+    } else {
+      double a[3], b[3], e[3];
+      for (int k = 0; k < 3; ++k) {
+        a[k] = x[1][k] - x[0][k];
+        b[k] = x[2][k] - x[0][k];
+        e[k] = x[3][k] - x[0][k];
+      }
+      double bc[3] = {b[1] * e[2] - b[2] * e[1], b[2] * e[0] - b[0] * e[2], b[0] * e[1] - b[1] * e[0]};
+      double ca[3] = {e[1] * a[2] - e[2] * a[1], e[2] * a[0] - e[0] * a[2], e[0] * a[1] - e[1] * a[0]};
+      double ab[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+      double det = 2 * (a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2]);
+      double la = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+      double lb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+      double le = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+      r2 = 0;
+      for (int k = 0; k < 3; ++k) {
+        double u = (la * bc[k] + lb * ca[k] + le * ab[k]) / det;
+        r2 += u * u;
+      }
+    }
+    out[c] = sqrt(r2) / sqrt(minl2);
+  }
+}
+
+int re_ratios(int dim, const double *P, const int32_t *cells, int64_t nc, double *out,
+              cudaStream_t s) {
+  DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
+  DM_ARG_CHECK(nc >= 0 && (nc == 0 || (P && cells && out)), "arguments");
+  if (nc == 0) return DM_OK;
+  if (dim == 3)
+    k_re_ratios<3><<<grid_for(nc, 256), 256, 0, s>>>(P, cells, nc, out);
+  else
+    k_re_ratios<2><<<grid_for(nc, 256), 256, 0, s>>>(P, cells, nc, out);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
 int simplex_metrics(int dim, const float *P, const int32_t *cells, int64_t nc,
                     double *vol, double *qual, cudaStream_t s) {
   DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
@@ -513,6 +577,347 @@ int laplacian_smooth(float *P, int64_t n, const int32_t *adj, int cap,
     set_error("laplacian: no convergence in %d iterations", max_iter);
     return DM_ERR_NOT_CONVERGED;
   }
+  return DM_OK;
+}
+
+}  // namespace dm
+
+namespace dm {
+
+// ---------------------------------------------------------------------------
+// do_any_overlap (geometry/utils.py:745-817): the centroid of every cell is
+// tested against every other cell in its 1-ring (the cells sharing one of its
+// vertices, vertex_to_entities 97-130).  The arithmetic follows the
+// reference operation by operation in FP64 with explicit round-to-nearest
+// intrinsics, so no multiply-add is contracted and every decision matches
+// the reference's double-precision evaluation:
+//   centroid      get_centroids 729-742: ((v0 + v1) + v2 [+ v3]) / (dim + 1)
+//   2D inclusion  vertex_in_entity2 657-679: barycentric a, b, c = 1 - a - b,
+//                 all three in [0, 1]
+//   3D inclusion  vertex_in_entity3 682-726: the five 4x4 determinants of
+//                 calc_4x4determinant (fast_geometry.cpp:482-495), each
+//                 summed left to right, must share one non-zero sign
+// A pair (ie, ele) is reported once per vertex the two cells share, as the
+// reference's loop over the vertices of ie does; pairs are ordered by ie,
+// then by the vertex slot in ie, then by ele.
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+// calc_4x4determinant on a row-major 4x4 matrix: 24 four-factor products,
+// each multiplied left to right, accumulated left to right with the signs
+// of the reference expression
+__device__ double det4x4_ref(const double *m) {
+  // {i0, i1, i2, i3, sign}
+  constexpr int T[24][5] = {
+      {12, 9, 6, 3, 1},    {8, 13, 6, 3, -1},   {12, 5, 10, 3, -1},  {4, 13, 10, 3, 1},
+      {8, 5, 14, 3, 1},    {4, 9, 14, 3, -1},   {12, 9, 2, 7, -1},   {8, 13, 2, 7, 1},
+      {12, 1, 10, 7, 1},   {0, 13, 10, 7, -1},  {8, 1, 14, 7, -1},   {0, 9, 14, 7, 1},
+      {12, 5, 2, 11, 1},   {4, 13, 2, 11, -1},  {12, 1, 6, 11, -1},  {0, 13, 6, 11, 1},
+      {4, 1, 14, 11, 1},   {0, 5, 14, 11, -1},  {8, 5, 2, 15, -1},   {4, 9, 2, 15, 1},
+      {8, 1, 6, 15, 1},    {0, 9, 6, 15, -1},   {4, 1, 10, 15, -1},  {0, 5, 10, 15, 1}};
+  double s = 0;
+#pragma unroll
+  for (int k = 0; k < 24; ++k) {
+    double t = dmul(dmul(dmul(m[T[k][0]], m[T[k][1]]), m[T[k][2]]), m[T[k][3]]);
+    s = k == 0 ? t : (T[k][4] > 0 ? dadd(s, t) : dsub(s, t));
+  }
+  return s;
+}
+
+__device__ __forceinline__ int sign_d(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
+
+template <int DIM>
+__device__ void centroid_ref(const double *X, const int32_t *c, double *cent) {
+  for (int d = 0; d < DIM; ++d) {
+    double s = X[(int64_t)c[0] * DIM + d];
+    for (int k = 1; k <= DIM; ++k) s = dadd(s, X[(int64_t)c[k] * DIM + d]);
+    cent[d] = __ddiv_rn(s, (double)(DIM + 1));
+  }
+}
+
+template <int DIM>
+__device__ bool inside_ref(const double *X, const int32_t *c, const double *q) {
+  if (DIM == 2) {
+    const double x1 = X[2 * (int64_t)c[0]], y1 = X[2 * (int64_t)c[0] + 1];
+    const double x2 = X[2 * (int64_t)c[1]], y2 = X[2 * (int64_t)c[1] + 1];
+    const double x3 = X[2 * (int64_t)c[2]], y3 = X[2 * (int64_t)c[2] + 1];
+    const double x = q[0], y = q[1];
+    const double den = dadd(dmul(dsub(y2, y3), dsub(x1, x3)), dmul(dsub(x3, x2), dsub(y1, y3)));
+    const double a =
+        __ddiv_rn(dadd(dmul(dsub(y2, y3), dsub(x, x3)), dmul(dsub(x3, x2), dsub(y, y3))), den);
+    const double b =
+        __ddiv_rn(dadd(dmul(dsub(y3, y1), dsub(x, x3)), dmul(dsub(x1, x3), dsub(y, y3))), den);
+    const double cc = dsub(dsub(1.0, a), b);
+    return 0 <= a && a <= 1 && 0 <= b && b <= 1 && 0 <= cc && cc <= 1;
+  } else {
+    double m[16];
+    for (int r = 0; r < 4; ++r) {
+      for (int d = 0; d < 3; ++d) m[4 * r + d] = X[3 * (int64_t)c[r] + d];
+      m[4 * r + 3] = 1.0;
+    }
+    const int s0 = sign_d(det4x4_ref(m));
+    int prev = s0;
+    for (int r = 0; r < 4; ++r) {
+      double save[3];
+      for (int d = 0; d < 3; ++d) {
+        save[d] = m[4 * r + d];
+        m[4 * r + d] = q[d];
+      }
+      const int s = sign_d(det4x4_ref(m));
+      for (int d = 0; d < 3; ++d) m[4 * r + d] = save[d];
+      if (s != prev) return false;
+      prev = s;
+    }
+    return s0 != 0;
+  }
+}
+
+__global__ void k_v2c_count(const int32_t *cells, int64_t ne, int64_t n, int32_t *cnt,
+                            int32_t *status) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ne;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = cells[i];
+    if (v < 0 || v >= n)
+      atomicOr(status, 1);
+    else
+      atomicAdd(&cnt[v], 1);
+  }
+}
+
+__global__ void k_v2c_fill(const int32_t *cells, int64_t ne, int nv, int64_t n,
+                           const int32_t *ptr, int32_t *cursor, int32_t *vtoe) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ne;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t v = cells[i];
+    if (v < 0 || v >= n) continue;
+    vtoe[ptr[v] + atomicAdd(&cursor[v], 1)] = (int32_t)(i / nv);
+  }
+}
+
+// each row ascending (insertion sort; rows are the cells around one vertex)
+__global__ void k_v2c_sort(int64_t n, const int32_t *ptr, int32_t *vtoe) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t b = ptr[v], e = ptr[v + 1];
+    for (int32_t i = b + 1; i < e; ++i) {
+      const int32_t x = vtoe[i];
+      int32_t j = i - 1;
+      while (j >= b && vtoe[j] > x) {
+        vtoe[j + 1] = vtoe[j];
+        --j;
+      }
+      vtoe[j + 1] = x;
+    }
+  }
+}
+
+// FILL = false: count the pairs of every cell; true: write them at ptr[ie]
+template <int DIM, bool FILL>
+__global__ void k_overlap(const double *X, const int32_t *cells, int64_t nc,
+                          const int32_t *vptr, const int32_t *vtoe, int32_t *cnt,
+                          const int32_t *cptr, int32_t *pairs) {
+  for (int64_t ie = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ie < nc;
+       ie += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t *c = cells + (DIM + 1) * ie;
+    double cent[DIM];
+    centroid_ref<DIM>(X, c, cent);
+    int32_t k = 0;
+    const int32_t base = FILL ? cptr[ie] : 0;
+    for (int s = 0; s <= DIM; ++s) {
+      const int32_t v = c[s];
+      for (int32_t j = vptr[v]; j < vptr[v + 1]; ++j) {
+        const int32_t ele = vtoe[j];
+        if (ele == ie) continue;
+        if (inside_ref<DIM>(X, cells + (int64_t)(DIM + 1) * ele, cent)) {
+          if (FILL) {
+            pairs[2 * (int64_t)(base + k)] = (int32_t)ie;
+            pairs[2 * (int64_t)(base + k) + 1] = ele;
+          }
+          ++k;
+        }
+      }
+    }
+    if (!FILL) cnt[ie] = k;
+  }
+}
+
+struct OverlapWs {
+  int32_t *vcnt, *vptr, *cursor, *vtoe, *ccnt, *cptr, *tmp, *status;
+};
+
+static size_t carve_overlap(Carve &c, int dim, int64_t n, int64_t nc, OverlapWs &w) {
+  w.vcnt = c.take<int32_t>(n + 1);
+  w.vptr = c.take<int32_t>(n + 1);
+  w.cursor = c.take<int32_t>(n + 1);
+  w.vtoe = c.take<int32_t>(nc * (dim + 1) + 1);
+  w.ccnt = c.take<int32_t>(nc + 1);
+  w.cptr = c.take<int32_t>(nc + 1);
+  w.tmp = c.take<int32_t>(scan_tmp_elems(n > nc ? n + 1 : nc + 1));
+  w.status = c.take<int32_t>(4);
+  return c.used;
+}
+
+size_t overlap_workspace(int dim, int64_t n, int64_t nc) {
+  Carve c(nullptr, 0);
+  OverlapWs w;
+  return carve_overlap(c, dim, n, nc, w) + 256;
+}
+
+int overlap_pairs(int dim, const double *X, int64_t n, const int32_t *cells, int64_t nc,
+                  int32_t *pairs, int64_t cap, int64_t *n_pairs, void *ws, size_t ws_bytes,
+                  cudaStream_t s) {
+  DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
+  DM_ARG_CHECK(n >= 0 && nc >= 0 && cap >= 0 && n_pairs, "arguments");
+  DM_ARG_CHECK(nc == 0 || (X && cells), "null points or cells");
+  DM_ARG_CHECK(cap == 0 || pairs, "null pairs");
+  *n_pairs = 0;
+  if (nc == 0) return DM_OK;
+  Carve c(ws, ws_bytes);
+  OverlapWs w;
+  carve_overlap(c, dim, n, nc, w);
+  if (!c.ok() || !ws) {
+    set_error("overlap_pairs: workspace %zu < required %zu", ws_bytes, c.used);
+    return DM_ERR_WORKSPACE;
+  }
+  const int nv = dim + 1;
+  const int64_t ne = nc * nv;
+  DM_CUDA_TRY(cudaMemsetAsync(w.vcnt, 0, sizeof(int32_t) * (n + 1), s));
+  DM_CUDA_TRY(cudaMemsetAsync(w.cursor, 0, sizeof(int32_t) * (n + 1), s));
+  DM_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int32_t) * 4, s));
+  k_v2c_count<<<grid_for(ne, 256), 256, 0, s>>>(cells, ne, n, w.vcnt, w.status);
+  int rc = exclusive_scan_i32(w.vcnt, w.vptr, n, w.tmp, s);
+  if (rc) return rc;
+  k_v2c_fill<<<grid_for(ne, 256), 256, 0, s>>>(cells, ne, nv, n, w.vptr, w.cursor, w.vtoe);
+  k_v2c_sort<<<grid_for(n, 128), 128, 0, s>>>(n, w.vptr, w.vtoe);
+  int32_t status = 0;
+  DM_CUDA_TRY(cudaMemcpyAsync(&status, w.status, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (status) {
+    set_error("overlap_pairs: a cell vertex is outside [0, %lld)", (long long)n);
+    return DM_ERR_ARG;
+  }
+  const int nb = grid_for(nc, 128);
+  if (dim == 3)
+    k_overlap<3, false><<<nb, 128, 0, s>>>(X, cells, nc, w.vptr, w.vtoe, w.ccnt, nullptr, nullptr);
+  else
+    k_overlap<2, false><<<nb, 128, 0, s>>>(X, cells, nc, w.vptr, w.vtoe, w.ccnt, nullptr, nullptr);
+  rc = exclusive_scan_i32(w.ccnt, w.cptr, nc, w.tmp, s);
+  if (rc) return rc;
+  int32_t total = 0;
+  DM_CUDA_TRY(cudaMemcpyAsync(&total, w.cptr + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaStreamSynchronize(s));
+  *n_pairs = total;
+  if (total > cap) {
+    set_error("overlap_pairs: %d pairs exceed capacity %lld", total, (long long)cap);
+    return DM_ERR_CAPACITY;
+  }
+  if (total == 0) return DM_OK;
+  if (dim == 3)
+    k_overlap<3, true><<<nb, 128, 0, s>>>(X, cells, nc, w.vptr, w.vtoe, nullptr, w.cptr, pairs);
+  else
+    k_overlap<2, true><<<nb, 128, 0, s>>>(X, cells, nc, w.vptr, w.vtoe, nullptr, w.cptr, pairs);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+}  // namespace dm
+
+namespace dm {
+
+// ---------------------------------------------------------------------------
+// Cell quality of the reference's benchmark reports (benchmarks/helpers.py
+// print_stats_2d / print_stats_3d, which take meshplex's cell_quality and
+// q_min_sin_dihedral_angles), in FP64:
+//   quality   = dim * inradius / circumradius   (1 for the regular simplex)
+//             inradius = dim * volume / (sum of facet measures)
+//   3D        sin of the dihedral angle at edge (i, j), whose two faces are
+//             the ones opposite the other two vertices k, l:
+//               sin = 3 V |x_i - x_j| / (2 A_k A_l)
+//             min over the six edges / sin(regular) = min / (2 sqrt(2) / 3)
+template <int DIM>
+__global__ void k_cell_quality(const double *X, const int32_t *cells, int64_t nc,
+                               double *quality, double *min_sin) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    double x[DIM + 1][DIM];
+    for (int k = 0; k <= DIM; ++k) {
+      const int64_t v = cells[(DIM + 1) * c + k];
+      for (int d = 0; d < DIM; ++d) x[k][d] = X[v * DIM + d];
+    }
+    if (DIM == 2) {
+      double l[3];
+      for (int k = 0; k < 3; ++k) {
+        const double dx = x[(k + 1) % 3][0] - x[(k + 2) % 3][0];
+        const double dy = x[(k + 1) % 3][1] - x[(k + 2) % 3][1];
+        l[k] = sqrt(dx * dx + dy * dy);
+      }
+      const double area = 0.5 * fabs((x[1][0] - x[0][0]) * (x[2][1] - x[0][1]) -
+                                     (x[1][1] - x[0][1]) * (x[2][0] - x[0][0]));
+      const double r = 2 * area / (l[0] + l[1] + l[2]);
+      const double R = l[0] * l[1] * l[2] / (4 * area);
+      quality[c] = 2 * r / R;
+    } else {
+      double e[4][4][3];
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+          for (int d = 0; d < 3; ++d) e[i][j][d] = x[j][d] - x[i][d];
+      // facet areas: A[k] = area of the face opposite vertex k
+      double A[4];
+      for (int k = 0; k < 4; ++k) {
+        const int a = (k + 1) & 3, b = (k + 2) & 3, cc = (k + 3) & 3;
+        const double *u = e[a][b], *w = e[a][cc];
+        const double n0 = u[1] * w[2] - u[2] * w[1], n1 = u[2] * w[0] - u[0] * w[2],
+                     n2 = u[0] * w[1] - u[1] * w[0];
+        A[k] = 0.5 * sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+      }
+      const double *a = e[0][1], *b = e[0][2], *d = e[0][3];
+      const double det = a[0] * (b[1] * d[2] - b[2] * d[1]) - a[1] * (b[0] * d[2] - b[2] * d[0]) +
+                         a[2] * (b[0] * d[1] - b[1] * d[0]);
+      const double V = fabs(det) / 6;
+      const double r = 3 * V / (A[0] + A[1] + A[2] + A[3]);
+      // circumradius: |u| with u = (la (b x d) + lb (d x a) + ld (a x b)) / (2 det)
+      const double la = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+      const double lb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+      const double ld = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      double R2 = 0;
+      for (int k = 0; k < 3; ++k) {
+        const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+        const double bd = b[k1] * d[k2] - b[k2] * d[k1];
+        const double da = d[k1] * a[k2] - d[k2] * a[k1];
+        const double ab = a[k1] * b[k2] - a[k2] * b[k1];
+        const double u = (la * bd + lb * da + ld * ab) / (2 * det);
+        R2 += u * u;
+      }
+      quality[c] = 3 * r / sqrt(R2);
+      if (min_sin) {
+        double m = 1e300;
+        for (int i = 0; i < 4; ++i)
+          for (int j = i + 1; j < 4; ++j) {
+            int k = -1, l = -1;
+            for (int q = 0; q < 4; ++q)
+              if (q != i && q != j) (k < 0 ? k : l) = q;
+            const double *g = e[i][j];
+            const double len = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            m = fmin(m, 3 * V * len / (2 * A[k] * A[l]));
+          }
+        min_sin[c] = m / (2 * 1.4142135623730951 / 3);
+      }
+    }
+  }
+}
+
+int cell_quality(int dim, const double *X, const int32_t *cells, int64_t nc, double *quality,
+                 double *min_sin, cudaStream_t s) {
+  DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
+  DM_ARG_CHECK(nc >= 0 && (nc == 0 || (X && cells && quality)), "arguments");
+  if (nc == 0) return DM_OK;
+  if (dim == 3)
+    k_cell_quality<3><<<grid_for(nc, 128), 128, 0, s>>>(X, cells, nc, quality, min_sin);
+  else
+    k_cell_quality<2><<<grid_for(nc, 128), 128, 0, s>>>(X, cells, nc, quality, nullptr);
+  DM_LAUNCH_CHECK();
   return DM_OK;
 }
 

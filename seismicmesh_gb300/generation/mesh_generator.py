@@ -390,12 +390,10 @@ class _Engine:
         self.counters[N.CNT_CELLS] = nk
         return self.filter(domain, geps)
 
-    def delete_boundary_entities(self, min_qual, verbose):
-        """geometry.delete_boundary_entities (geometry/utils.py:440-469):
-        drop cells touching a boundary vertex whose quality is < min_qual"""
+    def boundary_delete_mask(self, min_qual):
+        """cells touching a boundary vertex whose quality is < min_qual
+        (geometry/utils.py:456-459), as a device bool mask over the kept cells"""
         nk = int(self.counters[N.CNT_KEPT].item())
-        if nk == 0:
-            return
         qual = D.empty((nk,), torch.float64)
         N.call("dm_simplex_metrics", self.dim, D.ptr(self.P), D.ptr(self.kept), nk,
                None, D.ptr(qual), D.stream_ptr())
@@ -403,7 +401,15 @@ class _Engine:
         bflag[self.boundary_vertices(N.CNT_KEPT).long()] = 1
         t = self.kept[:nk].long()
         touches = bflag[t].sum(1) > 0
-        delete = touches & (qual < min_qual)
+        return touches & (qual < min_qual)
+
+    def delete_boundary_entities(self, min_qual, verbose):
+        """geometry.delete_boundary_entities (geometry/utils.py:440-469):
+        drop cells touching a boundary vertex whose quality is < min_qual"""
+        nk = int(self.counters[N.CNT_KEPT].item())
+        if nk == 0:
+            return
+        delete = self.boundary_delete_mask(min_qual)
         if verbose:
             print("Deleting " + str(int(delete.sum().item())) + " poor quality boundary entities...", flush=True)
         keep = self.kept[:nk][~delete].clone()

@@ -22,7 +22,7 @@ from .. import _native as N
 # op codes of csrc/dm_sdf.cuh
 OP_DISK, OP_BALL, OP_RECT, OP_CUBE, OP_TORUS, OP_PRISM, OP_CYLINDER, OP_GRID = range(1, 9)
 OP_UNION, OP_INTERSECTION, OP_DIFFERENCE = 20, 21, 22
-XF_TRANSLATE, XF_RX, XF_RY, XF_RZ, XF_STRETCH = 1, 2, 4, 8, 16
+XF_TRANSLATE, XF_RX, XF_RY, XF_RZ, XF_STRETCH, XF_REPEAT = 1, 2, 4, 8, 16, 32
 
 
 def corners(bbox):
@@ -124,6 +124,7 @@ class _Program:
         self.dim = dim
         self.ops = []
         self.params = []
+        self.repeat = None  # period while a Repeat's domain is emitted
 
     def add(self, op, params, count=0, xf=0):
         off = len(self.params)
@@ -216,6 +217,9 @@ class _Primitive(_SDFBase):
 
     def _emit(self, prog):
         flags, tail = self._xform(prog)
+        if prog.repeat is not None:  # inside a Repeat: its period comes first
+            flags |= XF_REPEAT
+            tail = list(prog.repeat) + tail
         prog.add(self._op, list(self._prim_params()) + tail, 0, flags)
 
 
@@ -363,6 +367,8 @@ class GridSDF(_SDFBase):
         self.corners = None
 
     def _emit(self, prog):
+        if prog.repeat is not None:
+            raise NotImplementedError("a gridded SDF inside Repeat is not supported")
         n = list(self.values.shape) + [1] * (3 - self.dim)
         lo = [self.bbox[2 * k] for k in range(self.dim)] + [0.0] * (3 - self.dim)
         hi = [self.bbox[2 * k + 1] for k in range(self.dim)] + [1.0] * (3 - self.dim)
@@ -407,11 +413,9 @@ class Difference(_SetOp):
 
 
 class Repeat(_SDFBase):
-    """Periodic repetition of a domain inside a Cube (reference 283-297).
-
-    Accepted by the API for drop-in compatibility; its device program is not
-    implemented yet, so meshing with it raises.
-    """
+    """Periodic repetition of a domain inside a Cube (reference 283-297):
+    max(domain(mod(x + p/2, p) - p/2), Cube(bbox)(x)).  On the device the
+    periodic map is a transform of every primitive of the repeated domain."""
 
     def __init__(self, bbox, domain, period):
         self.bbox = bbox
@@ -422,7 +426,15 @@ class Repeat(_SDFBase):
         self.dim = 3
 
     def _emit(self, prog):
-        raise NotImplementedError("Repeat has no device SDF program yet")
+        if prog.repeat is not None:
+            raise NotImplementedError("nested Repeat is not supported")
+        prog.repeat = [float(v) for v in np.broadcast_to(self.period, (3,))]
+        try:
+            self.domain._emit(prog)
+        finally:
+            prog.repeat = None
+        self.parent._emit(prog)
+        prog.add(OP_INTERSECTION, [0.0], 2, 0)
 
 
 def _ddisk(p, xc, yc, r):

@@ -299,7 +299,61 @@ def reference_test_goldens():
     print(json.dumps(res, indent=1))
 
 
+def repeat_goldens():
+    """geometry.Repeat (signed_distance_functions.py:283-297) at random points"""
+    from SeismicMesh.geometry.signed_distance_functions import Repeat
+
+    rng = np.random.default_rng(41)
+    x = f32(rng.uniform(-1.2, 1.2, (5000, 3)))
+    bbox = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    cases = {
+        "ball": Repeat(bbox, SM.Ball([0.0, 0.0, 0.0], 0.12), [0.4, 0.4, 0.4]),
+        "ball_aniso": Repeat(bbox, SM.Ball([0.0, 0.0, 0.0], 0.1), [0.3, 0.5, 0.45]),
+        "union": Repeat(bbox, SM.Union([SM.Ball([0.0, 0.0, 0.0], 0.1), SM.Cube((-0.05, 0.05, -0.2, 0.2, -0.05, 0.05))]),
+                        [0.5, 0.5, 0.5]),
+    }
+    save("repeat.npz", x=x, **{k: v.eval(x) for k, v in cases.items()})
+
+
+def folded(p, t, dim, h, seed, k=6, scale=0.8):
+    """a mesh with overlapping cells: k interior vertices pushed by scale*h"""
+    rng = np.random.default_rng(seed)
+    p = p.copy()
+    bnd = set(G.get_boundary_vertices(t, dim=dim).tolist())
+    interior = np.array([v for v in range(len(p)) if v not in bnd])
+    pick = rng.choice(interior, k, replace=False)
+    d = rng.normal(size=(k, dim))
+    p[pick] += scale * h * d / np.linalg.norm(d, axis=1, keepdims=True)
+    return p
+
+
+def qa_goldens():
+    """mesh quality and linting: calc_re_ratios (geometry/utils.py:17-54),
+    do_any_overlap (745-817) and linter (820-872) on small meshes"""
+    import contextlib
+    import io
+
+    disk = np.load(os.path.join(HERE, "disk_h01.npz"))
+    ball = np.load(os.path.join(HERE, "iter_ball.npz"))
+    p2, t2 = disk["p"], disk["t"].astype(np.int64)
+    p3, t3 = ball["p0"], ball["t"].astype(np.int64)
+    out = dict(p2=p2, t2=t2, p3=p3, t3=t3)
+    out["re2"] = G.calc_re_ratios(p2, t2, dim=2)
+    out["re3"] = G.calc_re_ratios(p3, t3, dim=3)
+    out["f2"] = folded(p2, t2, 2, 0.1, 7, k=12, scale=1.6)
+    out["f3"] = folded(p3, t3, 3, 0.2, 8, scale=0.6)
+    sink = io.StringIO()
+    with contextlib.redirect_stdout(sink):
+        out["ov2"] = np.array(G.do_any_overlap(out["f2"], t2, dim=2), dtype=np.int64).reshape(-1, 2)
+        out["ov3"] = np.array(G.do_any_overlap(out["f3"], t3, dim=3), dtype=np.int64).reshape(-1, 2)
+        out["ov2_clean"] = np.array(G.do_any_overlap(p2, t2, dim=2), dtype=np.int64).reshape(-1, 2)
+        lp, lt = G.linter(out["f2"], t2, dim=2)
+    out["lint2_p"], out["lint2_t"] = lp, lt.astype(np.int64)
+    save("mesh_qa.npz", **out)
+
+
 if __name__ == "__main__":
     parts = sys.argv[1:] or ["main"]
     for part in parts:
-        {"main": main, "gradient": gradient_goldens, "reftests2": reference_test_goldens}[part]()
+        {"main": main, "gradient": gradient_goldens, "reftests2": reference_test_goldens,
+         "repeat": repeat_goldens, "qa": qa_goldens}[part]()

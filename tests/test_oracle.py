@@ -112,3 +112,41 @@ def test_reference_test_goldens_recorded():
     r = d["test_2dmesher_SDF"]
     assert np.allclose(r["ref_harness"], r["golden"], atol=r["atol"])
     assert min(d["test_2d_min_qual"]["ref_harness_min_quals"]) > 0.60
+
+
+def test_mesh_qa_restatement_matches_reference():
+    """re ratios, 1-ring overlaps (as multisets: the reference lists the cells
+    around a vertex in quicksort order) against the reference's outputs"""
+    from oracle import mesh_qa_np as Q
+
+    g = golden("mesh_qa.npz")
+    np.testing.assert_allclose(Q.calc_re_ratios(g["p2"], g["t2"], 2), g["re2"], rtol=1e-12)
+    np.testing.assert_allclose(Q.calc_re_ratios(g["p3"], g["t3"][:400], 3), g["re3"][:400], rtol=1e-10)
+    for key, dim in (("2", 2), ("3", 3)):
+        ov = Q.do_any_overlap(g["f" + key], g["t" + key], dim)
+        assert sorted(ov) == sorted(map(tuple, g["ov" + key].tolist()))
+    assert Q.do_any_overlap(g["p2"], g["t2"], 2) == []
+
+
+def test_kat_re_ratios_equilateral_pair():
+    """reference tests/test_geometry2.py:11-15: two equilateral-ish triangles"""
+    from oracle import mesh_qa_np as Q
+
+    points = np.array([[0, 0], [6, 0], [3, 3], [9, 3]], dtype=float)
+    cells = np.array([[3, 2, 1], [2, 0, 1]])
+    np.testing.assert_allclose(Q.calc_re_ratios(points, cells, 2), [0.70710678, 0.70710678], rtol=1e-8)
+    assert Q.do_any_overlap(points, cells, 2) == []
+
+
+def test_kat_cell_quality_regular_and_right_triangle():
+    from oracle import mesh_qa_np as Q
+
+    tri = np.array([[0.0, 0.0], [1.0, 0.0], [0.5, np.sqrt(3) / 2]])
+    q, _ = Q.cell_quality(tri, np.array([[0, 1, 2]]))
+    np.testing.assert_allclose(q, [1.0], rtol=1e-14)
+    q, _ = Q.cell_quality(np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]]), np.array([[0, 1, 2]]))
+    np.testing.assert_allclose(q, [2 * (2 - np.sqrt(2)) / 2 / (np.sqrt(2) / 2)], rtol=1e-14)
+    tet = np.array([[1.0, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])
+    q, s = Q.cell_quality(tet, np.array([[0, 1, 2, 3]]))
+    np.testing.assert_allclose(q, [1.0], rtol=1e-14)
+    np.testing.assert_allclose(s, [1.0], rtol=1e-14)

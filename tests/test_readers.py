@@ -58,3 +58,32 @@ def test_binary_reader_orders(tmp_path):
                 got, *_ = _read_bin(str(f), nz, nx, ny, bo, order, sort, "float32")
                 want = np.flipud(data.transpose(order))
                 np.testing.assert_array_equal(got, want)
+
+
+def test_vtk_writer_roundtrip(tmp_path):
+    from seismicmesh_gb300.io import read_vtk, write_vtk
+
+    rng = np.random.default_rng(5)
+    for dim, nv in ((2, 3), (3, 4)):
+        p = rng.random((50, dim))
+        t = rng.integers(0, 50, (80, nv))
+        f = tmp_path / f"m{dim}.vtk"
+        write_vtk(str(f), p, t, cell_data={"q": rng.random(80)})
+        pp, tt = read_vtk(str(f))
+        np.testing.assert_array_equal(pp[:, :dim], p)
+        np.testing.assert_array_equal(tt, t)
+        assert f.read_bytes().startswith(b"# vtk DataFile Version 3.0")
+
+
+def test_gmsh22_writer_roundtrip(tmp_path):
+    from seismicmesh_gb300.io import read_gmsh22, write_mesh
+
+    rng = np.random.default_rng(6)
+    for dim, nv in ((2, 3), (3, 4)):
+        p = rng.random((40, dim))
+        t = rng.integers(0, 40, (70, nv))
+        f = tmp_path / f"m{dim}.msh"
+        write_mesh(str(f), p, t)
+        pp, tt = read_gmsh22(str(f))
+        np.testing.assert_array_equal(pp[:, :dim], p)
+        np.testing.assert_array_equal(tt, t)
