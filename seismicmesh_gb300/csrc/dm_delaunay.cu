@@ -77,6 +77,14 @@ struct DTArgs {
   int32_t *l3_cnt;
   int32_t *esc;       // [n]
   int4 *esc_seed;     // [n]
+  // hull candidates (3D): vertices whose level-1 star was not closed,
+  // bucketed by coarse block (o_start: nullptr until they are built)
+  uint8_t *hullc;     // [n]
+  int32_t *o_cnt;     // [cap_blocks] counts, then fill cursors
+  int32_t *o_start;   // [cap_blocks + 1]
+  int *o_box;         // [cap_blocks * 6] order-preserving ints (f2o)
+  float4 *o_pts;      // [n] x, y, z, id bits
+  int use_o;          // hull scans read the hull candidates
   int32_t *cells;
   int64_t cap_cells_out;
   int64_t *counters;
@@ -107,6 +115,11 @@ static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
   a.l3_cnt = c.take<int32_t>((size_t)L3_BLOCKS * L3_WARPS * 4);
   a.esc = c.take<int32_t>(n);
   a.esc_seed = c.take<int4>(n);
+  a.hullc = c.take<uint8_t>(n);
+  a.o_cnt = c.take<int32_t>(a.cap_blocks);
+  a.o_start = c.take<int32_t>(a.cap_blocks + 1);
+  a.o_box = c.take<int>(a.cap_blocks * 6);
+  a.o_pts = c.take<float4>(n);
   return c.used;
 }
 
@@ -364,6 +377,62 @@ __global__ void k_block_boxes(const float *P, const GridParams *gp,
 }
 
 // ---------------------------------------------------------------------------
+// Hull candidates (3D).  Level 1 flags every vertex whose star it could not
+// close among its candidates (an open star, no seed, or over capacity).  A
+// vertex of the convex hull of the point set (symbolically perturbed, as
+// every predicate here is) lies on the hull of any subset that contains it,
+// so its level-1 star is open: the flagged set holds every hull vertex.  The
+// maximum of an affine function over the points is reached at a hull
+// vertex, so a half-space that holds no flagged vertex holds no point at
+// all.  Hull scans (face queries whose half-space has no point near the
+// face) read the flagged vertices, bucketed by coarse block with tight
+// boxes, instead of every cell of every block the half-space crosses.
+__device__ __forceinline__ int block_of_cell(const GridParams &g, int c) {
+  const int cx = c % g.dims[0], cy = (c / g.dims[0]) % g.dims[1],
+            cz = c / (g.dims[0] * g.dims[1]);
+  return cx / g.bs + g.bdims[0] * (cy / g.bs + g.bdims[1] * (cz / g.bs));
+}
+
+__global__ void k_hc_init(const GridParams *gp, int32_t *o_cnt, int *o_box) {
+  const int nb = gp->nblocks;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    o_cnt[b] = 0;
+    for (int k = 0; k < 3; ++k) {
+      o_box[6 * b + k] = f2o(FLT_MAX);
+      o_box[6 * b + 3 + k] = f2o(-FLT_MAX);
+    }
+  }
+}
+
+__global__ void k_hc_count(int64_t n, const uint8_t *hullc, const int32_t *cell_of,
+                           const GridParams *gp, int32_t *o_cnt) {
+  const GridParams g = *gp;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x)
+    if (hullc[v]) atomicAdd(&o_cnt[block_of_cell(g, cell_of[v])], 1);
+}
+
+__global__ void k_hc_fill(int64_t n, const float *P, const uint8_t *hullc,
+                          const int32_t *cell_of, const GridParams *gp,
+                          const int32_t *o_start, int32_t *o_cur, int *o_box,
+                          float4 *o_pts) {
+  const GridParams g = *gp;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    if (!hullc[v]) continue;
+    const int b = block_of_cell(g, cell_of[v]);
+    const int pos = o_start[b] + atomicAdd(&o_cur[b], 1);
+    float x[3];
+    load_pt<3>(P, (int)v, x);
+    o_pts[pos] = make_float4(x[0], x[1], x[2], __int_as_float((int)v));
+    for (int k = 0; k < 3; ++k) {
+      atomicMin(&o_box[6 * b + k], f2o(x[k]));
+      atomicMax(&o_box[6 * b + 3 + k], f2o(x[k]));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Level 1: shared-memory neighbourhoods
 template <int DIM>
 struct L1 {};
@@ -395,6 +464,7 @@ struct WarpL1 {
   int nc, ntri, nopen;
   int flags;
   float reff;
+  int capped;  // the candidate radius was cut below the covered radius
 };
 
 __device__ __forceinline__ uint32_t pack3(int a, int b, int c) {
@@ -758,6 +828,7 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
   if (lane == 0) {
     S.nc = 0;
     S.reff = bmax < 0 ? 0.f : reff;
+    S.capped = bmax != 15 || rcnt < rcov;
   }
   __syncwarp();
   if (bmax < 0) return;
@@ -1030,6 +1101,16 @@ __device__ __forceinline__ uint32_t seed2L(const WarpL1<2> &S, const float *P,
   return 0xffffffffu;
 }
 
+// Level-1 outcome counts of the 3D kernel, compiled in only with
+// -DDM_L2_STATS: {no seed, open star, capacity, certification failed, stars,
+// candidates, stars with a capped candidate radius, link triangles}
+#ifdef DM_L2_STATS
+static __device__ unsigned long long g_l1s[8];
+#define L1S_ADD(i, v) atomicAdd(&g_l1s[i], (unsigned long long)(v))
+#else
+#define L1S_ADD(i, v) ((void)0)
+#endif
+
 // escalation record: (p, a, b, c) global ids; c < 0 means "no seed";
 // bit 30 of p marks a certified seed cell.
 __device__ __forceinline__ void escalate(const DTArgs &A, int p, int4 seed,
@@ -1057,7 +1138,16 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
     gather_l1<3>(S, A, g, ip, px, lane, L1<3>::K);
     int ovf = 0;
     uint32_t seed = S.nc >= 3 ? seed3L(S, A.P, ip, lane, ovf, W) : 0xffffffffu;
+    if (lane == 0) {
+      L1S_ADD(4, 1);
+      L1S_ADD(5, S.nc);
+      L1S_ADD(6, S.capped);
+    }
     if (seed == 0xffffffffu) {
+      if (lane == 0) {
+        L1S_ADD(0, 1);
+        A.hullc[ip] = 1;
+      }
       escalate(A, ip, make_int4(ip, -1, -1, -1), lane);
       continue;
     }
@@ -1138,6 +1228,11 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
     }
     allok = __all_sync(0xffffffffu, allok);
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+    if (lane == 0) {
+      L1S_ADD(7, S.ntri);
+      if (!allok) L1S_ADD(hull ? 1 : (S.flags ? 2 : 3), 1);
+      if (hull || S.flags) A.hullc[ip] = 1;
+    }
     if (!allok) {
       unsigned m = S.flags ? 0u : __ballot_sync(0xffffffffu, cert_any >= 0);
       int4 sd;
@@ -1674,12 +1769,42 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     R.kind = 0;
     rex = 1;
   }
+  // no point near the face: if no hull candidate lies in H+, no point does;
+  // a candidate that does bounds the region of the regular search
+  bool h_empty = false;
+  if (R.kind == 0 && A.use_o && !A.dbg_full) {
+    if (lane == 0) L2S_ADD(1, 1);
+    for (int bid = lane; bid < g.nblocks; bid += 32) {
+      const int s0 = A.o_start[bid], s1 = A.o_start[bid + 1];
+      if (s0 == s1) continue;
+      float blo[3], bhi[3];
+      for (int k = 0; k < 3; ++k) {
+        blo[k] = o2f(A.o_box[6 * bid + k]);
+        bhi[k] = o2f(A.o_box[6 * bid + 3 + k]);
+      }
+      if (!region_hits3(R, blo, bhi)) continue;
+      for (int i = s0; i < s1; ++i) {
+        const float4 q = A.o_pts[i];
+        consider3(A, F, __float_as_int(q.w), q, best, bx, ovf, W);
+      }
+    }
+    best = tourney3(A, F, best, ovf, W);
+    if (best >= 0) {
+      load_pt<3>(A.P, best, bx);
+      make_region3(R, F.p, a, b, n, nn, la, lb, bx);
+      region3_floats(R);
+    } else {
+      h_empty = true;
+    }
+  }
   if (lane == 0) {
     if (R.kind == 1) L2S_ADD(4, 1);
     if (R.kind == 2) L2S_ADD(5, 1);
     if (large) L2S_ADD(6, 1);
   }
-  if (R.kind != 0) {
+  if (h_empty) {
+    // every point in H+ would have shown a hull candidate in H+
+  } else if (R.kind != 0) {
     int lo[3], hi[3];
     int64_t ncell = 1;
     for (int k = 0; k < 3; ++k) {
@@ -2719,6 +2844,7 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   // kernels still run on the single-cell grid and stay bounded)
   int64_t nwb = (n + L1_WARPS - 1) / L1_WARPS;
   int g1 = (int)std::min<int64_t>(nwb, (int64_t)kSMs * 16);
+  if (dim == 3) DM_CUDA_TRY(cudaMemsetAsync(a.hullc, 0, n, s));
   prof_mark(0, s);
   if (dim == 3)
     k_star3_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
@@ -2726,6 +2852,21 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
     k_star2_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
   DM_LAUNCH_CHECK();
   prof_mark(1, s);
+  int launches = 14;
+  if (dim == 3) {
+    // hull candidates bucketed by coarse block
+    DM_CUDA_TRY(cudaMemsetAsync(a.o_cnt, 0, sizeof(int32_t) * a.cap_blocks, s));
+    k_hc_init<<<grid_for(a.cap_blocks, 256), 256, 0, s>>>(a.gp, a.o_cnt, a.o_box);
+    k_hc_count<<<nb, 256, 0, s>>>(n, a.hullc, a.cell_of, a.gp, a.o_cnt);
+    rc = exclusive_scan_i32(a.o_cnt, a.o_start, a.cap_blocks, a.scan_tmp, s);
+    if (rc) return rc;
+    DM_CUDA_TRY(cudaMemsetAsync(a.o_cnt, 0, sizeof(int32_t) * a.cap_blocks, s));
+    k_hc_fill<<<nb, 256, 0, s>>>(n, pts, a.hullc, a.cell_of, a.gp, a.o_start, a.o_cnt,
+                                 a.o_box, a.o_pts);
+    DM_LAUNCH_CHECK();
+    a.use_o = 1;
+    launches += 6;
+  }
   int g2 = kSMs * 8;
   if (dim == 3) {
     k_star3_l2<<<g2, 32 * L2_WARPS, 0, s>>>(a);
@@ -2737,7 +2878,7 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   DM_LAUNCH_CHECK();
   prof_mark(2, s);
   if (g_prof_on && g_prof_n < kProfMax) ++g_prof_n;
-  note_launches(13);
+  note_launches(launches);
   return DM_OK;
 }
 
@@ -2769,7 +2910,9 @@ extern "C" int dmdbg_face_query(int32_t dim, const float *pts, int64_t n,
   return dmdbg_face_query_mode(dim, pts, n, ws, ws_bytes, faces, m, out, stream, 0);
 }
 
-// mode 1: exhaustive half-space scan for every face (ground truth, 3D)
+// mode 1: exhaustive half-space scan for every face (ground truth, 3D);
+// mode 2: hull scans through the hull candidates of the last dm_delaunay
+// call on the same points and workspace (3D)
 extern "C" int dmdbg_face_query_mode(int32_t dim, const float *pts, int64_t n,
                                      void *ws, size_t ws_bytes, const int32_t *faces,
                                      int32_t m, int32_t *out, void *stream, int32_t mode) {
@@ -2782,7 +2925,8 @@ extern "C" int dmdbg_face_query_mode(int32_t dim, const float *pts, int64_t n,
   a.n = n;
   a.P = pts;
   a.dbg_vertex = -1;
-  a.dbg_full = mode;
+  a.dbg_full = mode == 1;
+  a.use_o = mode == 2 && dim == 3;
   k_debug_gq<<<(m + 3) / 4, 128, 0, (cudaStream_t)stream>>>(a, faces, m, out);
   DM_LAUNCH_CHECK();
   return DM_OK;
@@ -2906,6 +3050,17 @@ extern "C" int dmprof_slow_counters(unsigned long long *out8) {
 
 // Debug aid: copy level-2 statistics of the last dm_delaunay (stars < 2^17,
 // 8 values each); returns 0 when the statistics are not compiled in.
+extern "C" int dmprof_l1_stats(unsigned long long *out8) {
+#ifdef DM_L2_STATS
+  cudaMemcpyFromSymbol(out8, dm::g_l1s, sizeof(unsigned long long) * 8);
+  unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaMemcpyToSymbol(dm::g_l1s, z, sizeof(z));
+  return 1;
+#else
+  (void)out8;
+  return 0;
+#endif
+}
 extern "C" int dmprof_l2_stats(unsigned long long *out, int64_t nstars) {
 #ifdef DM_L2_STATS
   if (nstars > dm::kL2StatStars) nstars = dm::kL2StatStars;

@@ -151,10 +151,15 @@ def test_face_queries_match_exhaustive_half_space_scan(cuda, kind):
             for (u, v) in ((o[0], o[1]), (o[1], o[2]), (o[2], o[0]), (o[1], o[0]), (o[2], o[1]), (o[0], o[2])):
                 faces.append((c[i], u, v))
     faces = np.array(faces)
-    got, _ = _face_queries(P, faces, 0, grid)
     want, _ = _face_queries(P, faces, 1, grid)
-    bad = np.nonzero(got != want)[0]
-    assert len(bad) == 0, (len(bad), faces[bad[:5]].tolist(), got[bad[:5]].tolist(), want[bad[:5]].tolist())
+    # mode 0: scans of every block; mode 2: hull scans through the hull
+    # candidates that level 1 flagged
+    for mode in (0, 2):
+        got, _ = _face_queries(P, faces, mode, grid)
+        bad = np.nonzero(got != want)[0]
+        assert len(bad) == 0, (mode, len(bad), faces[bad[:5]].tolist(), got[bad[:5]].tolist(),
+                               want[bad[:5]].tolist())
+    assert (want < 0).sum() > 100  # hull faces are among the queries
 
 
 @pytest.mark.gpu
