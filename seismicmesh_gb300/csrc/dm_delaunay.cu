@@ -84,6 +84,9 @@ struct DTArgs {
   int32_t *o_start;   // [cap_blocks + 1]
   int *o_box;         // [cap_blocks * 6] order-preserving ints (f2o)
   float4 *o_pts;      // [n] x, y, z, id bits
+  float4 *o_tab;      // [2 * cap_blocks] non-empty candidate blocks: (lo, start bits),
+                      // (hi, count bits)
+  int32_t *o_ntab;    // [1] entries of o_tab
   int use_o;          // hull scans read the hull candidates
   int32_t *cells;
   int64_t cap_cells_out;
@@ -120,6 +123,8 @@ static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
   a.o_start = c.take<int32_t>(a.cap_blocks + 1);
   a.o_box = c.take<int>(a.cap_blocks * 6);
   a.o_pts = c.take<float4>(n);
+  a.o_tab = c.take<float4>(2 * a.cap_blocks);
+  a.o_ntab = c.take<int32_t>(4);
   return c.used;
 }
 
@@ -429,6 +434,22 @@ __global__ void k_hc_fill(int64_t n, const float *P, const uint8_t *hullc,
       atomicMin(&o_box[6 * b + k], f2o(x[k]));
       atomicMax(&o_box[6 * b + 3 + k], f2o(x[k]));
     }
+  }
+}
+
+// table of the non-empty candidate blocks (tight box, range); hull scans
+// walk it instead of every block index
+__global__ void k_hc_table(const GridParams *gp, const int32_t *o_start, const int *o_box,
+                           float4 *o_tab, int32_t *o_ntab) {
+  const int nb = gp->nblocks;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    const int s0 = o_start[b], s1 = o_start[b + 1];
+    if (s0 == s1) continue;
+    const int e = atomicAdd(o_ntab, 1);
+    o_tab[2 * e] = make_float4(o2f(o_box[6 * b]), o2f(o_box[6 * b + 1]), o2f(o_box[6 * b + 2]),
+                               __int_as_float(s0));
+    o_tab[2 * e + 1] = make_float4(o2f(o_box[6 * b + 3]), o2f(o_box[6 * b + 4]),
+                                   o2f(o_box[6 * b + 5]), __int_as_float(s1 - s0));
   }
 }
 
@@ -1736,6 +1757,31 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   // after a tournament every lane holds the same winner: reload its point
   best = tourney3(A, F, best, ovf, W);
   if (best >= 0) load_pt<3>(A.P, best, bx);
+  // no point near the face: if no hull candidate lies in H+, no point does
+  // (a hull face); a candidate that does bounds the region of the search
+  bool h_empty = false;
+  if (best < 0 && A.use_o && !A.dbg_full) {
+    if (lane == 0) L2S_ADD(1, 1);
+    Region3 H;
+    make_region3(H, F.p, a, b, n, nn, la, lb, nullptr);
+    region3_floats(H);
+    const int ntab = *A.o_ntab;
+    for (int e = lane; e < ntab; e += 32) {
+      const float4 t0 = A.o_tab[2 * e], t1 = A.o_tab[2 * e + 1];
+      const float blo[3] = {t0.x, t0.y, t0.z}, bhi[3] = {t1.x, t1.y, t1.z};
+      if (!region_hits3(H, blo, bhi)) continue;
+      const int s0 = __float_as_int(t0.w), s1 = s0 + __float_as_int(t1.w);
+      for (int i = s0; i < s1; ++i) {
+        const float4 q = A.o_pts[i];
+        consider3(A, F, __float_as_int(q.w), q, best, bx, ovf, W);
+      }
+    }
+    best = tourney3(A, F, best, ovf, W);
+    if (best >= 0)
+      load_pt<3>(A.P, best, bx);
+    else
+      h_empty = true;
+  }
 #ifdef DM_L2_STATS
   const long long tr_t0 = clock64();
   const int tr_local = best;
@@ -1751,6 +1797,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   bool large = R.kind == 0;
   for (int k = 0; k < 3 && !large; ++k)
     large = (R.hi[k] - R.lo[k]) * g.inv_cs > 5.0;
+  large = large && !h_empty;
   if (large) {
     for (int t = lane; t < 125; t += 32) {
       int dx = t % 5 - 2, dy = (t / 5) % 5 - 2, dz = t / 25 - 2;
@@ -1768,34 +1815,6 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   if (A.dbg_full) {
     R.kind = 0;
     rex = 1;
-  }
-  // no point near the face: if no hull candidate lies in H+, no point does;
-  // a candidate that does bounds the region of the regular search
-  bool h_empty = false;
-  if (R.kind == 0 && A.use_o && !A.dbg_full) {
-    if (lane == 0) L2S_ADD(1, 1);
-    for (int bid = lane; bid < g.nblocks; bid += 32) {
-      const int s0 = A.o_start[bid], s1 = A.o_start[bid + 1];
-      if (s0 == s1) continue;
-      float blo[3], bhi[3];
-      for (int k = 0; k < 3; ++k) {
-        blo[k] = o2f(A.o_box[6 * bid + k]);
-        bhi[k] = o2f(A.o_box[6 * bid + 3 + k]);
-      }
-      if (!region_hits3(R, blo, bhi)) continue;
-      for (int i = s0; i < s1; ++i) {
-        const float4 q = A.o_pts[i];
-        consider3(A, F, __float_as_int(q.w), q, best, bx, ovf, W);
-      }
-    }
-    best = tourney3(A, F, best, ovf, W);
-    if (best >= 0) {
-      load_pt<3>(A.P, best, bx);
-      make_region3(R, F.p, a, b, n, nn, la, lb, bx);
-      region3_floats(R);
-    } else {
-      h_empty = true;
-    }
   }
   if (lane == 0) {
     if (R.kind == 1) L2S_ADD(4, 1);
@@ -2863,9 +2882,12 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
     DM_CUDA_TRY(cudaMemsetAsync(a.o_cnt, 0, sizeof(int32_t) * a.cap_blocks, s));
     k_hc_fill<<<nb, 256, 0, s>>>(n, pts, a.hullc, a.cell_of, a.gp, a.o_start, a.o_cnt,
                                  a.o_box, a.o_pts);
+    DM_CUDA_TRY(cudaMemsetAsync(a.o_ntab, 0, sizeof(int32_t), s));
+    k_hc_table<<<grid_for(a.cap_blocks, 256), 256, 0, s>>>(a.gp, a.o_start, a.o_box, a.o_tab,
+                                                           a.o_ntab);
     DM_LAUNCH_CHECK();
     a.use_o = 1;
-    launches += 6;
+    launches += 7;
   }
   int g2 = kSMs * 8;
   if (dim == 3) {
@@ -3003,6 +3025,17 @@ extern "C" int dmdbg_escalations(int32_t dim, int64_t n, void *ws, size_t ws_byt
   carve_dt(c, a, dim, n);
   cudaMemcpyAsync(esc_out, a.esc, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
   cudaMemcpyAsync(seed_out, a.esc_seed, sizeof(int4) * n, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Debug aid: copy the hull-candidate flags of the last 3D dm_delaunay call.
+extern "C" int dmdbg_hull_candidates(int64_t n, void *ws, size_t ws_bytes, uint8_t *out,
+                                     void *stream) {
+  using namespace dm;
+  Carve c(ws, ws_bytes);
+  DTArgs a;
+  carve_dt(c, a, 3, n);
+  cudaMemcpyAsync(out, a.hullc, n, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
