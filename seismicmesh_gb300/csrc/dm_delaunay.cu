@@ -469,7 +469,7 @@ struct L1<2> {
 constexpr int L1_WARPS = 4;
 // minimum resident blocks per SM requested from the register allocator
 #ifndef DM_L1_MINB
-#define DM_L1_MINB 1
+#define DM_L1_MINB 4  // 128 registers: 4 blocks per SM measured 23 % faster than 1
 #endif
 #ifndef DM_L2_MINB
 #define DM_L2_MINB 5  // 96 registers: 5 blocks per SM measured 2-8 % faster than 4
@@ -627,9 +627,11 @@ static __device__ __noinline__ int gw3L(const WarpL1<3> &S, const float *P, int 
   // permanent terms of A x B for the error bound (16u, as orient3 filters)
   const float pnx = fabsf(A.y * B.z) + fabsf(A.z * B.y), pny = fabsf(A.z * B.x) + fabsf(A.x * B.z),
               pnz = fabsf(A.x * B.y) + fabsf(A.y * B.x);
-  uint32_t pos = 0;
+  uint32_t pos = 0, und = 0;
   float bk = FLT_MAX;
   int bj = -1, bg = 0x7fffffff;
+  // filtered orientations; the undecided ones go to one exact call site
+  // below (keeps the unrolled loop small)
 #pragma unroll
   for (int s = 0; s < L1<3>::PER; ++s) {
     int j = lane + 32 * s;
@@ -638,18 +640,26 @@ static __device__ __noinline__ int gw3L(const WarpL1<3> &S, const float *P, int 
       float den = Y.x * nx + Y.y * ny + Y.z * nz;
       int o = filter_sign(den, fabsf(Y.x) * pnx + fabsf(Y.y) * pny + fabsf(Y.z) * pnz,
                           16.0f * DMP_U32);
-      if (o == 0) o = o3L_exact(S, P, ip, a, b, j, W);
-      if (o > 0) {
-        pos |= 1u << s;
-        float tau = (Y.w - 2.f * (Y.x * cx + Y.y * cy + Y.z * cz)) / den;
-        if (!(tau == tau) || !(den > 0.f)) tau = FLT_MAX;
-        int g = S.id[j];
-        if (bj < 0 || tau < bk || (tau == bk && g < bg)) {
-          bk = tau;
-          bj = j;
-          bg = g;
-        }
-      }
+      if (o > 0) pos |= 1u << s;
+      if (o == 0) und |= 1u << s;
+    }
+  }
+  while (und) {
+    const int s = __ffs(und) - 1;
+    und &= und - 1;
+    if (o3L_exact(S, P, ip, a, b, lane + 32 * s, W) > 0) pos |= 1u << s;
+  }
+  for (uint32_t m = pos; m; m &= m - 1) {
+    const int j = lane + 32 * (__ffs(m) - 1);
+    float4 Y = S.c[j];
+    float den = Y.x * nx + Y.y * ny + Y.z * nz;
+    float tau = (Y.w - 2.f * (Y.x * cx + Y.y * cy + Y.z * cz)) / den;
+    if (!(tau == tau) || !(den > 0.f)) tau = FLT_MAX;
+    int g = S.id[j];
+    if (bj < 0 || tau < bk || (tau == bk && g < bg)) {
+      bk = tau;
+      bj = j;
+      bg = g;
     }
   }
   warp_argmin(bk, bj, bg);
@@ -659,14 +669,20 @@ static __device__ __noinline__ int gw3L(const WarpL1<3> &S, const float *P, int 
     SphereRows R;
     sphere_rows(R, A, B, S.c[bj]);
     int found = -1;
+    uint32_t und2 = 0;
 #pragma unroll
     for (int s = 0; s < L1<3>::PER; ++s) {
       int j = lane + 32 * s;
       if (found < 0 && (pos >> s & 1u) && j != bj) {
         int v = sphere_filter(R, S.c[j]);
-        if (v == 0) v = is3L_exact(S, P, ip, a, b, bj, j, ovf, W);
         if (v < 0) found = j;
+        if (v == 0) und2 |= 1u << s;
       }
+    }
+    while (found < 0 && und2) {
+      const int s = __ffs(und2) - 1;
+      und2 &= und2 - 1;
+      if (is3L_exact(S, P, ip, a, b, bj, lane + 32 * s, ovf, W) < 0) found = lane + 32 * s;
     }
     unsigned m = __ballot_sync(0xffffffffu, found >= 0);
     if (!m) return bj;
@@ -800,6 +816,11 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
   rcov = rcov * (1.f - 1e-5f);
   float rcnt = rcov;
   int bmax = -1;
+  // the first pass also stores its points: when they fit (the usual case)
+  // no second pass is needed
+  if (lane == 0) S.nc = 0;
+  __syncwarp();
+  bool stored = false;
   for (int round = 0; round < 6 && bmax < 0; ++round, rcnt *= (1.f / 16.f)) {
     const float rc2 = rcnt * rcnt;
     int bins[16];
@@ -828,12 +849,24 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
           int bidx = min(15, (int)(sqrtf(d2s) / rcnt * 16.f));
 #pragma unroll
           for (int k = 0; k < 16; ++k) bins[k] += (k == bidx);
+          if (round == 0) {
+            const int slot = atomicAdd(&S.nc, 1);
+            if (slot < L1<DIM>::CAP) {
+              float r[3] = {0.f, 0.f, 0.f};
+              for (int k = 0; k < DIM; ++k) r[k] = xq[k] - px[k];
+              S.c[slot] = make_float4(r[0], r[1], r[2],
+                                      DIM == 3 ? r[0] * r[0] + r[1] * r[1] + r[2] * r[2]
+                                               : r[0] * r[0] + r[1] * r[1]);
+              S.id[slot] = q;
+            }
+          }
         }
       }
     }
     for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
     if (total <= L1<DIM>::CAP) {
       bmax = 15;
+      stored = round == 0;
       break;
     }
     int cum = 0;
@@ -846,13 +879,18 @@ __device__ __forceinline__ void gather_l1(WarpL1<DIM> &S, const DTArgs &A, const
     if (bmax >= 0) break;
   }
   const float reff = bmax == 15 ? rcnt : rcnt * (bmax + 1) / 16.f * (1.f - 1e-5f);
+  __syncwarp();
   if (lane == 0) {
-    S.nc = 0;
+    if (!stored) S.nc = 0;
     S.reff = bmax < 0 ? 0.f : reff;
     S.capped = bmax != 15 || rcnt < rcov;
   }
   __syncwarp();
   if (bmax < 0) return;
+  if (stored) {
+    fixed_coords<DIM>(S, A, px, lane, g.gfix);
+    return;
+  }
   const float rc2 = rcnt * rcnt;
   for (int t = lane; t < NCELL; t += 32) {
     int d0 = t % W - K, d1 = (t / W) % W - K, d2 = DIM == 3 ? t / (W * W) - K : 0;
@@ -1126,10 +1164,12 @@ __device__ __forceinline__ uint32_t seed2L(const WarpL1<2> &S, const float *P,
 // -DDM_L2_STATS: {no seed, open star, capacity, certification failed, stars,
 // candidates, stars with a capped candidate radius, link triangles}
 #ifdef DM_L2_STATS
-static __device__ unsigned long long g_l1s[8];
+static __device__ unsigned long long g_l1s[16];
 #define L1S_ADD(i, v) atomicAdd(&g_l1s[i], (unsigned long long)(v))
+#define L1S_CLOCK() clock64()
 #else
 #define L1S_ADD(i, v) ((void)0)
+#define L1S_CLOCK() 0ll
 #endif
 
 // escalation record: (p, a, b, c) global ids; c < 0 means "no seed";
@@ -1156,10 +1196,15 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
     if (A.dup[ip]) continue;
     float px[3];
     load_pt<3>(A.P, ip, px);
+    [[maybe_unused]] long long t0 = L1S_CLOCK();
     gather_l1<3>(S, A, g, ip, px, lane, L1<3>::K);
+    [[maybe_unused]] long long t1 = L1S_CLOCK();
     int ovf = 0;
     uint32_t seed = S.nc >= 3 ? seed3L(S, A.P, ip, lane, ovf, W) : 0xffffffffu;
+    [[maybe_unused]] long long t2 = L1S_CLOCK();
     if (lane == 0) {
+      L1S_ADD(8, t1 - t0);
+      L1S_ADD(9, t2 - t1);
       L1S_ADD(4, 1);
       L1S_ADD(5, S.nc);
       L1S_ADD(6, S.capped);
@@ -1238,6 +1283,8 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
       }
       __syncwarp();
     }
+    [[maybe_unused]] long long t3 = L1S_CLOCK();
+    if (lane == 0) L1S_ADD(10, t3 - t2);
     // certification
     bool allok = !hull && !S.flags;
     int cert_any = -1;
@@ -1268,6 +1315,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
       escalate(A, ip, sd, lane);
       continue;
     }
+    if (lane == 0) L1S_ADD(11, L1S_CLOCK() - t3);
     // emit cells owned by p (p has the smallest index)
     for (int t0 = 0; t0 < S.ntri; t0 += 32) {
       int t = t0 + lane;
@@ -3085,8 +3133,8 @@ extern "C" int dmprof_slow_counters(unsigned long long *out8) {
 // 8 values each); returns 0 when the statistics are not compiled in.
 extern "C" int dmprof_l1_stats(unsigned long long *out8) {
 #ifdef DM_L2_STATS
-  cudaMemcpyFromSymbol(out8, dm::g_l1s, sizeof(unsigned long long) * 8);
-  unsigned long long z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaMemcpyFromSymbol(out8, dm::g_l1s, sizeof(unsigned long long) * 16);
+  unsigned long long z[16] = {};
   cudaMemcpyToSymbol(dm::g_l1s, z, sizeof(z));
   return 1;
 #else
