@@ -472,7 +472,7 @@ constexpr int L1_WARPS = 4;
 #define DM_L1_MINB 4  // 128 registers: 4 blocks per SM measured 23 % faster than 1
 #endif
 #ifndef DM_L2_MINB
-#define DM_L2_MINB 5  // 96 registers: 5 blocks per SM measured 2-8 % faster than 4
+#define DM_L2_MINB 4  // 128 registers: measured 10 % faster than 5 blocks per SM (96)
 #endif
 
 template <int DIM>
@@ -1538,7 +1538,11 @@ __device__ __forceinline__ int insph_face3(const Face3 &F, const float *c, const
   return dmp::insph3_sos_tail(F.p, F.a, F.b, c, d, W);
 }
 
+#ifdef DM_C3_NOINLINE
+static __device__ __noinline__ void consider3(const DTArgs &A, const Face3 &F, int j,
+#else
 __device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j,
+#endif
                                           float4 q, int &best, float *bx, int &ovf,
                                           dmp::ExactScratch *W) {
   if (j == F.ip || j == F.ia || j == F.ib) return;
