@@ -55,6 +55,7 @@ constexpr int kNoFix = -100000;
 // level-3 star storage: per-warp slots in the workspace
 constexpr int L3_CAP_TRI = 4096, L3_CAP_OPEN = 2048, L3_WARPS = 4, L3_BLOCKS = 76;
 constexpr int kCntL3 = 11;  // counters slot: stars deferred to level 3
+constexpr int kCntL2Next = 12;  // counters slot: next escalated star for level 2 (3D)
 
 struct DTArgs {
   int dim;
@@ -2582,8 +2583,13 @@ __global__ void __launch_bounds__(32 * L2_WARPS, DM_L2_MINB) k_star3_l2(DTArgs A
   auto &Q1 = sm1[w];
   const GridParams g = *A.gp;
   const int64_t nesc = A.counters[DM_CNT_ESCALATED];
-  for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
-       k += (int64_t)gridDim.x * L2_WARPS) {
+  // stars are taken one at a time from a shared counter: their costs vary by
+  // orders of magnitude, so a static split leaves a long tail
+  for (;;) {
+    unsigned long long kk = 0;
+    if (lane == 0) kk = atomicAdd((unsigned long long *)&A.counters[kCntL2Next], 1ull);
+    const int64_t k = (int64_t)__shfl_sync(0xffffffffu, kk, 0);
+    if (k >= nesc) break;
 #ifdef DM_L2_STATS
     long long t_start = clock64();
     if (lane < 8) g_l2w[blockIdx.x * L2_WARPS + w][lane] = 0;
