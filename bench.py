@@ -311,15 +311,17 @@ def run_ours(args, world, rank, local):
     max_ms = reduce_max(total_ms, world, "nccl")
     value = world * n * args.steps / (max_ms / 1000.0)
 
-    # roofline of the dominant kernel (level-1 star kernel of dm_delaunay):
-    # algorithmic bytes per launch = points read (16 B each) + cells written
-    # (16 B each) + candidate grid reads (4 B per point for the sorted ids and
-    # 8 B per cell range), i.e. 16 n + 16 T + 4 n + 8 n_cells_grid ~ 16 T + 28 n
+    # roofline of the dominant work, the star kernels of dm_delaunay (levels 1
+    # and 2 together build one triangulation; 98 % of the device time):
+    # algorithmic bytes per triangulation = points read (16 B each) + cells
+    # written (16 B each) + candidate grid reads (4 B per point for the sorted
+    # ids and 8 B per cell range), i.e. 16 n + 16 T + 4 n + 8 n_cells_grid
+    # ~ 16 T + 28 n
     l1_ms = l1_total / max(l_calls, 1)
     l2_ms = l2_total / max(l_calls, 1)
     alg_bytes = 16 * n_cells + 28 * n
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (l1_ms / 1000.0) / 1e9
+    achieved = alg_bytes / ((l1_ms + l2_ms) / 1000.0) / 1e9
 
     e2e = None
     if not args.no_e2e:
@@ -379,7 +381,7 @@ def run_ours(args, world, rank, local):
             },
             "roofline": {
                 "bound": "hbm",
-                "kernel": "k_star3_l1 (vertex-star Delaunay, level 1)",
+                "kernel": "k_star3_l1 + k_star3_l2 (vertex-star Delaunay, levels 1 and 2)",
                 "achieved": achieved,
                 "peak": peak,
                 "peak_kind": peak_kind,
@@ -387,7 +389,8 @@ def run_ours(args, world, rank, local):
                 "frac": achieved / peak,
                 "traffic": measured_traffic(),
                 "alg_bytes_per_launch": alg_bytes,
-                "avg_launch_ms": l1_ms,
+                "avg_launch_ms": l1_ms + l2_ms,
+                "level1_ms": l1_ms,
                 "level2_ms": l2_ms,
             },
             "phases_ms": {"step_ms_min": min(step_ms), "step_ms_max": max(step_ms)},
@@ -401,18 +404,25 @@ def run_ours(args, world, rank, local):
 
 PROFILE_L1 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
                           "k_star3_l1_ball_h002.md")
+PROFILE_L2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                          "k_star3_l2_ball_h002.md")
 
 
 def measured_traffic():
-    """DRAM bytes (read + write) per k_star3_l1 launch from the committed ncu
-    summary of this workload (the line 'dram_bytes_per_launch: N'), or None"""
-    try:
-        for line in open(PROFILE_L1):
-            if line.strip().startswith("dram_bytes_per_launch:"):
-                return int(line.split(":")[1].strip().replace(",", ""))
-    except OSError:
-        pass
-    return None
+    """DRAM bytes (read + write) of one k_star3_l1 and one k_star3_l2 launch
+    from the committed ncu summaries of this workload (the lines
+    'dram_bytes_per_launch: N'), or None"""
+    total = 0
+    for path in (PROFILE_L1, PROFILE_L2):
+        try:
+            vals = [int(line.split(":")[1].strip().replace(",", "")) for line in open(path)
+                    if line.strip().startswith("dram_bytes_per_launch:")]
+        except OSError:
+            return None
+        if not vals:
+            return None
+        total += vals[0]
+    return total
 
 
 def ncu_case(args):
