@@ -322,6 +322,7 @@ def run_ours(args, world, rank, local):
     alg_bytes = 16 * n_cells + 28 * n
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / ((l1_ms + l2_ms) / 1000.0) / 1e9
+    it_roof = iteration_roofline(n, n_cells, int(c[N.CNT_EDGES]), max_ms / args.steps, peak)
 
     e2e = None
     if not args.no_e2e:
@@ -393,6 +394,9 @@ def run_ours(args, world, rank, local):
                 "level1_ms": l1_ms,
                 "level2_ms": l2_ms,
             },
+            "roofline_iteration": it_roof,
+            "delaunay": {"stars_per_s": n / ((l1_ms + l2_ms) / 1000.0),
+                         "level1_ms": l1_ms, "level2_ms": l2_ms},
             "phases_ms": {"step_ms_min": min(step_ms), "step_ms_max": max(step_ms)},
             "gpu_launches": int(launches),
             "clocks": clocks.summary(),
@@ -406,6 +410,26 @@ PROFILE_L1 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles"
                           "k_star3_l1_ball_h002.md")
 PROFILE_L2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
                           "k_star3_l2_ball_h002.md")
+
+
+def iteration_roofline(n, n_cells, n_edges, ms_per_step, peak, dim=3):
+    """Roofline of a whole DistMesh iteration with the compulsory bytes of its
+    per-iteration arrays (scalar sizing, no grid bytes): the cell table read
+    twice (edge build and centroid filter), the unique edges written and
+    read once, and the positions/forces passes,
+        B_iter = 2 * 4 (d + 1) T + 2 * 8 E + 6 * 4 d N."""
+    b_iter = 2 * 4 * (dim + 1) * n_cells + 2 * 8 * n_edges + 6 * 4 * dim * n
+    achieved = b_iter / (ms_per_step / 1000.0) / 1e9
+    return {
+        "bound": "hbm",
+        "scope": "one DistMesh iteration (graph replay)",
+        "alg_bytes_per_iteration": b_iter,
+        "bytes_per_point_iteration": b_iter / n,
+        "achieved": achieved,
+        "peak": peak,
+        "unit": "GB/s",
+        "frac": achieved / peak,
+    }
 
 
 def measured_traffic():
