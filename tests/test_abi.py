@@ -163,3 +163,48 @@ def test_sdf_program_encoding():
     r = sm.Rectangle((0.0, 1.0, 0.0, 1.0), rotate=[0.3, 0, 0], translate=[0.1, 0.2])
     op = r.program().ops[0]
     assert op[0] == 3 and op[3] == (1 | 2)  # translate + 2D rotation
+
+
+def test_qa_entry_points_reject_bad_arguments():
+    """argument checks of the mesh-QA entry points run before any device
+    work: bad dimension, negative sizes, missing pointers, tiny workspace"""
+    import ctypes
+
+    L = N.lib()
+    k = ctypes.c_int64(-1)
+    assert L.dm_overlap_pairs(4, None, 10, None, 5, None, 0, ctypes.byref(k), None, 0, None) == N.DM_ERR_ARG
+    assert b"dim" in L.dm_last_error()
+    assert L.dm_overlap_pairs(2, None, 10, None, -1, None, 0, ctypes.byref(k), None, 0, None) == N.DM_ERR_ARG
+    assert L.dm_overlap_pairs(3, None, 10, None, 5, None, 0, ctypes.byref(k), None, 0, None) == N.DM_ERR_ARG
+    # no cells: nothing to do, no pairs
+    assert L.dm_overlap_pairs(2, None, 0, None, 0, None, 0, ctypes.byref(k), None, 0, None) == N.DM_OK
+    assert k.value == 0
+    ws = N.c_sz(0)
+    assert L.dm_overlap_workspace_size(3, 1000, 5000, ws) == N.DM_OK and ws.value > 0
+    # a workspace below the size asked for is refused by name
+    fake = ctypes.c_void_p(256)
+    assert L.dm_overlap_pairs(3, fake, 1000, fake, 5000, fake, 10, ctypes.byref(k), fake, 16, None) \
+        == N.DM_ERR_WORKSPACE
+    assert b"workspace" in L.dm_last_error()
+    assert L.dm_radius_edge_ratios(5, None, None, 3, None, None) == N.DM_ERR_ARG
+    assert L.dm_radius_edge_ratios(2, None, None, 3, None, None) == N.DM_ERR_ARG
+    assert L.dm_radius_edge_ratios(2, None, None, 0, None, None) == N.DM_OK
+    assert L.dm_cell_quality(1, None, None, 3, None, None, None) == N.DM_ERR_ARG
+    assert L.dm_cell_quality(3, None, None, 3, None, None, None) == N.DM_ERR_ARG
+    assert L.dm_cell_quality(3, None, None, 0, None, None, None) == N.DM_OK
+
+
+def test_qa_python_wrappers_check_shapes():
+    import pytest
+
+    from seismicmesh_gb300 import geometry as G
+
+    with pytest.raises(ValueError):
+        G.do_any_overlap(np.zeros((4, 2)), np.zeros((2, 4), dtype=int), dim=2)
+    with pytest.raises(ValueError):
+        G.calc_re_ratios(np.zeros((4, 2)), np.zeros((2, 3), dtype=int), dim=4)
+    with pytest.raises(ValueError):
+        G.cell_quality(np.zeros((4, 4)), np.zeros((2, 5), dtype=int))
+    # empty meshes need no device
+    assert G.do_any_overlap(np.zeros((0, 2)), np.zeros((0, 3), dtype=int), dim=2) == []
+    assert len(G.calc_re_ratios(np.zeros((0, 3)), np.zeros((0, 4), dtype=int), dim=3)) == 0
