@@ -150,3 +150,13 @@ def test_kat_cell_quality_regular_and_right_triangle():
     q, s = Q.cell_quality(tet, np.array([[0, 1, 2, 3]]))
     np.testing.assert_allclose(q, [1.0], rtol=1e-14)
     np.testing.assert_allclose(s, [1.0], rtol=1e-14)
+
+
+def test_cell_quality_2d_is_the_reference_simp_qual():
+    """in 2D the benchmark quality 2 r / R is the reference's simp_qual
+    (geometry/utils.py:252-274): pinned to its outputs on the disk mesh"""
+    from oracle import mesh_qa_np as Q
+
+    g = golden("disk_h01.npz")
+    q, _ = Q.cell_quality(g["p"], g["t"])
+    np.testing.assert_allclose(q, g["qual"], rtol=1e-10)
