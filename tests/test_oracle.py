@@ -160,3 +160,18 @@ def test_cell_quality_2d_is_the_reference_simp_qual():
     g = golden("disk_h01.npz")
     q, _ = Q.cell_quality(g["p"], g["t"])
     np.testing.assert_allclose(q, g["qual"], rtol=1e-10)
+
+
+def test_min_sin_dihedral_against_reference_dihedral_angles():
+    """the 3D measure min sin(dihedral) / (2 sqrt(2) / 3) from the reference's
+    own calc_dihedral_angles (fast_geometry.cpp:351-418) outputs"""
+    from oracle import mesh_qa_np as Q
+
+    g = golden("fast_geometry.npz")
+    p, t = g["points"], g["cells"]
+    vol = np.abs(np.einsum("ij,ij->i", p[t[:, 1]] - p[t[:, 0]],
+                           np.cross(p[t[:, 2]] - p[t[:, 0]], p[t[:, 3]] - p[t[:, 0]])))
+    ok = vol > 1e-12  # flat cells have no meaningful angles
+    _, s = Q.cell_quality(p, t[ok])
+    ref = np.sin(g["dihedral"].reshape(-1, 6)[ok]).min(1) / (2 * np.sqrt(2) / 3)
+    np.testing.assert_allclose(s, ref, rtol=1e-8, atol=1e-12)
