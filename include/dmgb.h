@@ -149,7 +149,9 @@ int dm_adjacency(int32_t dim, int64_t n, const int32_t *cells,
                  int32_t adj_cap, int32_t *deg, int64_t *counters,
                  void *workspace, size_t workspace_bytes, void *stream);
 /* Drop-in unique_edges: edges int32[m][2] -> sorted unique (min,max) pairs.
- * Needs the vertex count bound n (max index + 1). */
+ * Needs the vertex count bound n (max index + 1).  An index outside [0, n)
+ * is never used as an address: the call returns DM_ERR_ARG (the output is
+ * then unspecified). */
 int dm_unique_edges_workspace_size(int64_t n, int64_t m, size_t *bytes);
 int dm_unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
                     int64_t *n_out_host, void *workspace,
@@ -173,6 +175,10 @@ int dm_unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
  * Nothing has to be zero beforehand: each call clears the counters it uses.
  * One scratch exists per device, so calls that overlap in time on the same
  * device (two streams or two host threads) race on it: serialise them.
+ * The looked-up address is kept for the life of the process: a
+ * cudaDeviceReset after the first call is not supported (the address may
+ * then be stale).  Out-of-range indices return DM_ERR_ARG as in
+ * dm_unique_edges.
  * Synchronises `stream` to read the output count, like dm_unique_edges. */
 int dm_unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
                             int32_t *out, int64_t *n_out_host, void *stream);
@@ -239,6 +245,10 @@ int dm_improve_level_set(int32_t dim, float *points, const int32_t *ids,
  * selection of sliver_removal (generation/mesh_generator.py:222-274). */
 int dm_dihedral_angles(const float *points, const int32_t *cells, int64_t nc,
                        double *angles, void *stream);
+/* calc_dihedral_angles (fast_geometry.cpp:351-418) on caller FP64 points
+ * double[n][3], FP64 throughout as in the reference. */
+int dm_dihedral_angles_f64(const double *points, const int32_t *cells, int64_t nc,
+                           double *angles, void *stream);
 int dm_circumsphere_grad(const double *p0, const double *p1, const double *p2,
                          const double *p3, int64_t m, double *grad,
                          void *stream);
@@ -352,9 +362,17 @@ int dm_overlap_workspace_size(int32_t dim, int64_t n, int64_t nc, size_t *bytes)
 int dm_overlap_pairs(int32_t dim, const double *points, int64_t n, const int32_t *cells,
                      int64_t nc, int32_t *pairs, int64_t cap, int64_t *n_pairs,
                      void *workspace, size_t workspace_bytes, void *stream);
+/* simp_vol / simp_qual (geometry/utils.py:175-201, 252-274): signed volume
+ * and 2 r / R of the first three vertices; volume or quality may be NULL.
+ * dm_simplex_metrics reads engine points (float[n][4] in 3D, float[n][2] in
+ * 2D); dm_simplex_metrics_f64 reads caller FP64 points double[n][dim] and
+ * stays in FP64 throughout, as the reference does. */
 int dm_simplex_metrics(int32_t dim, const float *points, const int32_t *cells,
                        int64_t nc, double *volume, double *quality,
                        void *stream);
+int dm_simplex_metrics_f64(int32_t dim, const double *points, const int32_t *cells,
+                           int64_t nc, double *volume, double *quality,
+                           void *stream);
 
 /* laplacian2_fixed_point (geometry/utils.py:494-547) for 2D points
  * float[n][2] (device, updated in place): interior vertices (boundary_flags

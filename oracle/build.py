@@ -17,8 +17,15 @@ def build_oracle_c():
     return LIB
 
 
+def reference_dir():
+    """the reference checkout: $SEISMICMESH_REF, else a directory named
+    `reference` beside this repository"""
+    return os.environ.get("SEISMICMESH_REF",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
+
+
 def build_ref():
-    ref = os.environ.get("SEISMICMESH_REF", "/root/reference")
+    ref = reference_dir()
     if not os.path.isdir(ref):
         return None
     try:

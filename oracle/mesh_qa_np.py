@@ -120,3 +120,31 @@ def cell_quality(p, t):
                     sines.append(3 * V * np.linalg.norm(x[i] - x[j]) / (2 * A[k] * A[l2]))
             s[c] = min(sines) / (2 * np.sqrt(2) / 3)
     return q, s
+
+
+def cell_quality_vec(p, t):
+    """Vectorised cell_quality for large meshes: the same textbook measures,
+    dim * inradius / circumradius and (3D) the minimum sine of the dihedral
+    angles normalised to the regular tetrahedron, in float64."""
+    p = np.asarray(p, dtype=np.float64)
+    t = np.asarray(t, dtype=np.int64)
+    dim = p.shape[1]
+    x = p[t]                                     # [m, dim+1, dim]
+    a = x[:, 1:] - x[:, :1]
+    rhs = 0.5 * (a * a).sum(-1)
+    R = np.linalg.norm(np.linalg.solve(a, rhs[..., None])[..., 0], axis=1)
+    if dim == 2:
+        l = [np.linalg.norm(x[:, (k + 1) % 3] - x[:, (k + 2) % 3], axis=1) for k in range(3)]
+        area = 0.5 * np.abs(a[:, 0, 0] * a[:, 1, 1] - a[:, 0, 1] * a[:, 1, 0])
+        return 2 * (2 * area / sum(l)) / R, None
+    faces = [[j for j in range(4) if j != k] for k in range(4)]
+    A = [0.5 * np.linalg.norm(np.cross(x[:, f[1]] - x[:, f[0]], x[:, f[2]] - x[:, f[0]]), axis=1)
+         for f in faces]
+    V = np.abs(np.linalg.det(a)) / 6
+    q = 3 * (3 * V / sum(A)) / R
+    s = np.full(len(t), np.inf)
+    for i in range(4):
+        for j in range(i + 1, 4):
+            k, l2 = [m for m in range(4) if m not in (i, j)]
+            s = np.minimum(s, 3 * V * np.linalg.norm(x[:, i] - x[:, j], axis=1) / (2 * A[k] * A[l2]))
+    return q, s / (2 * np.sqrt(2) / 3)

@@ -25,7 +25,9 @@ import scipy.sparse.linalg as spla
 from scipy.spatial import Delaunay
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("SEISMICMESH_REF", "/root/reference")
+# the reference checkout: $SEISMICMESH_REF, else `reference` beside this repository
+REF = os.environ.get("SEISMICMESH_REF",
+                     os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 REF_BUILD = os.path.join(HERE, "_ref")
 
 

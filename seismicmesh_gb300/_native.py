@@ -111,6 +111,7 @@ SIGNATURES = {
     "dm_sizing_eval": (c_int, [ctypes.POINTER(Sizing), c_p, c_i64, c_int, c_p, c_p]),
     "dm_improve_level_set": (c_int, [c_int, c_p, c_p, c_i64, ctypes.POINTER(SdfProgram), c_f, c_p]),
     "dm_dihedral_angles": (c_int, [c_p, c_p, c_i64, c_p, c_p]),
+    "dm_dihedral_angles_f64": (c_int, [c_p, c_p, c_i64, c_p, c_p]),
     "dm_circumsphere_grad": (c_int, [c_p, c_p, c_p, c_p, c_i64, c_p, c_p]),
     "dm_dihedral_flags": (c_int, [c_p, c_p, c_i64, c_int, c_f, c_f, c_p, c_p, c_p]),
     "dm_sliver_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
@@ -124,6 +125,7 @@ SIGNATURES = {
         [c_int, c_p, c_p, c_i64, c_p, c_i64, c_int, c_p, ctypes.POINTER(c_i64), c_p, c_sz, c_p],
     ),
     "dm_simplex_metrics": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
+    "dm_simplex_metrics_f64": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_p]),
     "dm_size_from_velocity": (
         c_int,
         [c_p, c_i64, c_i64, c_p, c_d, c_d, c_d, c_d, c_d, c_d, c_d, c_d, c_d, c_d,

@@ -37,6 +37,8 @@ int improve_level_set(int dim, float *P, const int32_t *ids, int64_t m,
                       const dm_sdf_program *sdf, float deps, cudaStream_t s);
 int dihedral_angles(const float *P, const int32_t *cells, int64_t nc,
                     double *ang, cudaStream_t s);
+int dihedral_angles_f64(const double *X, const int32_t *cells, int64_t nc,
+                        double *ang, cudaStream_t s);
 int circumsphere_grad(const double *p0, const double *p1, const double *p2,
                       const double *p3, int64_t m, double *g, cudaStream_t s);
 int dihedral_flags(const float *P, const int32_t *cells, int64_t cap,
@@ -78,6 +80,8 @@ int overlap_pairs(int dim, const double *X, int64_t n, const int32_t *cells, int
                   cudaStream_t s);
 int simplex_metrics(int dim, const float *P, const int32_t *cells, int64_t nc,
                     double *vol, double *qual, cudaStream_t s);
+int simplex_metrics_f64(int dim, const double *X, const int32_t *cells, int64_t nc,
+                        double *vol, double *qual, cudaStream_t s);
 size_t laplacian_workspace(int64_t n);
 struct SizeParams {
   double scale, vp_water;
@@ -102,7 +106,7 @@ extern "C" {
 
 int dm_version(void) { return 10000; }
 const char *dm_last_error(void) { return dm::last_error(); }
-int dm_abi_count(void) { return 45; }
+int dm_abi_count(void) { return 47; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
   dmp::ExactScratch W;
@@ -248,6 +252,10 @@ int dm_dihedral_angles(const float *points, const int32_t *cells, int64_t nc,
                        double *angles, void *stream) {
   return dm::dihedral_angles(points, cells, nc, angles, S(stream));
 }
+int dm_dihedral_angles_f64(const double *points, const int32_t *cells, int64_t nc,
+                           double *angles, void *stream) {
+  return dm::dihedral_angles_f64(points, cells, nc, angles, S(stream));
+}
 int dm_circumsphere_grad(const double *p0, const double *p1, const double *p2,
                          const double *p3, int64_t m, double *grad,
                          void *stream) {
@@ -331,6 +339,11 @@ int dm_simplex_metrics(int32_t dim, const float *points, const int32_t *cells,
                        int64_t nc, double *volume, double *quality,
                        void *stream) {
   return dm::simplex_metrics(dim, points, cells, nc, volume, quality, S(stream));
+}
+int dm_simplex_metrics_f64(int32_t dim, const double *points, const int32_t *cells,
+                           int64_t nc, double *volume, double *quality,
+                           void *stream) {
+  return dm::simplex_metrics_f64(dim, points, cells, nc, volume, quality, S(stream));
 }
 
 int dm_laplacian_workspace_size(int64_t n, size_t *bytes) {

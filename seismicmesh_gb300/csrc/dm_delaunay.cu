@@ -1266,6 +1266,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
       }
       if (S.flags) break;
     }
+#ifdef DM_DEBUG_VERTEX
     if (ip == A.dbg_vertex && A.dbg) {
       // [nc, ntri, hull, flags, reff bits, ids[nc]..., tri[ntri] (3 ids each)]
       if (lane == 0) {
@@ -1284,6 +1285,7 @@ __global__ void __launch_bounds__(32 * L1_WARPS, DM_L1_MINB) k_star3_l1(DTArgs A
       }
       __syncwarp();
     }
+#endif
     [[maybe_unused]] long long t3 = L1S_CLOCK();
     if (lane == 0) L1S_ADD(10, t3 - t2);
     // certification
@@ -2603,6 +2605,7 @@ __global__ void __launch_bounds__(32 * L2_WARPS, DM_L2_MINB) k_star3_l2(DTArgs A
     }
     const bool done = walk3(A, g, ip, seed, lane, ovf, W, S);
     if (ovf) flag_or(A.counters, DM_FLAG_EXACT_OVERFLOW);
+#ifdef DM_DEBUG_VERTEX
     if (ip == A.dbg_vertex && A.dbg) {
       // level-2 walk of the watched vertex: [1000] ntri, [1002..1004] seed,
       // [1008 + 3t ..] triangles in walk order
@@ -2619,6 +2622,7 @@ __global__ void __launch_bounds__(32 * L2_WARPS, DM_L2_MINB) k_star3_l2(DTArgs A
       }
       __syncwarp();
     }
+#endif
 #ifdef DM_L2_STATS
     if (lane == 0 && k < kL2StatStars) {
       g_l2s[k][0] = clock64() - t_start;
@@ -3099,10 +3103,18 @@ extern "C" int dmdbg_hull_candidates(int64_t n, void *ws, size_t ws_bytes, uint8
 
 // Debug aid: make the next dm_delaunay calls dump the level-1 state of one
 // vertex into dbg (device, >= 8 + 128 + 3*128 ints); vertex -1 disables.
+// The dumps are compiled in only with -DDM_DEBUG_VERTEX; otherwise the call
+// returns DM_ERR_ARG.
 extern "C" int dmdbg_watch_vertex(int32_t vertex, int32_t *dbg) {
+#ifdef DM_DEBUG_VERTEX
   dm::g_dbg_vertex = vertex;
   dm::g_dbg = dbg;
   return 0;
+#else
+  (void)vertex;
+  (void)dbg;
+  return DM_ERR_ARG;
+#endif
 }
 
 // Timing of the star kernels of the dm_delaunay calls made while enabled:

@@ -523,7 +523,22 @@ __device__ __forceinline__ T dihedral(const T *p0, const T *p1, const T *p2,
   return acos((d23 - d12 * d13) / (m12 * m13));
 }
 
-__global__ void k_dihedral(const float *P, const int32_t *cells, int64_t nc,
+// vertex v of a cell as FP64: engine points (float4 rows) or caller FP64
+// points (3 doubles per row, as the reference's numpy arrays)
+__device__ __forceinline__ void load_xyz(const float *P, int64_t v, double *x) {
+  float4 q = __ldg(reinterpret_cast<const float4 *>(P) + v);
+  x[0] = q.x;
+  x[1] = q.y;
+  x[2] = q.z;
+}
+__device__ __forceinline__ void load_xyz(const double *X, int64_t v, double *x) {
+  x[0] = X[3 * v];
+  x[1] = X[3 * v + 1];
+  x[2] = X[3 * v + 2];
+}
+
+template <typename PT>
+__global__ void k_dihedral(const PT *P, const int32_t *cells, int64_t nc,
                            double *ang) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc * 6;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -531,12 +546,7 @@ __global__ void k_dihedral(const float *P, const int32_t *cells, int64_t nc,
     int e = (int)(i % 6);
     double x[4][3];
     int vid[4] = {kDhE[e][0], kDhE[e][1], kDhE[5 - e][0], kDhE[5 - e][1]};
-    for (int k = 0; k < 4; ++k) {
-      float4 q = __ldg(reinterpret_cast<const float4 *>(P) + cells[4 * c + vid[k]]);
-      x[k][0] = q.x;
-      x[k][1] = q.y;
-      x[k][2] = q.z;
-    }
+    for (int k = 0; k < 4; ++k) load_xyz(P, cells[4 * c + vid[k]], x[k]);
     ang[i] = dihedral<double>(x[0], x[1], x[2], x[3]);
   }
 }
@@ -860,7 +870,16 @@ int improve_level_set(int dim, float *P, const int32_t *ids, int64_t m,
 
 int dihedral_angles(const float *P, const int32_t *cells, int64_t nc,
                     double *ang, cudaStream_t s) {
-  k_dihedral<<<grid_for(nc * 6, 256), 256, 0, s>>>(P, cells, nc, ang);
+  if (nc == 0) return DM_OK;
+  k_dihedral<float><<<grid_for(nc * 6, 256), 256, 0, s>>>(P, cells, nc, ang);
+  DM_LAUNCH_CHECK();
+  return DM_OK;
+}
+
+int dihedral_angles_f64(const double *X, const int32_t *cells, int64_t nc,
+                        double *ang, cudaStream_t s) {
+  if (nc == 0) return DM_OK;
+  k_dihedral<double><<<grid_for(nc * 6, 256), 256, 0, s>>>(X, cells, nc, ang);
   DM_LAUNCH_CHECK();
   return DM_OK;
 }

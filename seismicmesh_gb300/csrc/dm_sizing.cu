@@ -76,12 +76,19 @@ int limgrad(const int32_t *dims, double elen, double dfdx, int imax, double *f,
 // ---------------------------------------------------------------------------
 // unique_edges (geometry/cpp/fast_geometry.cpp:30-77): (min, max) pairs,
 // sorted lexicographically, duplicates removed.  Counting sort by the first
-// key, then each bucket is sorted and deduplicated on the second key.
-__global__ void k_ue_count(const int32_t *e, int64_t m, int32_t *cnt,
-                           int32_t *key, int32_t *slot) {
+// key, then each bucket is sorted and deduplicated on the second key.  An
+// index outside [0, n) is skipped and recorded in *bad, so a malformed edge
+// list can never write outside the workspace; the host returns DM_ERR_ARG.
+__global__ void k_ue_count(const int32_t *e, int64_t m, int64_t n, int32_t *cnt,
+                           int32_t *key, int32_t *slot, int32_t *bad) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * blockDim.x) {
     int a = e[2 * i], b = e[2 * i + 1];
+    if (a < 0 || b < 0 || a >= n || b >= n) {
+      key[i] = -1;
+      atomicExch(bad, 1);
+      continue;
+    }
     int lo = min(a, b);
     key[i] = lo;
     slot[i] = atomicAdd(&cnt[lo], 1);
@@ -93,17 +100,22 @@ __global__ void k_ue_scatter(const int32_t *e, int64_t m, const int32_t *start,
                              int32_t *val) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * blockDim.x) {
+    int k = key[i];
+    if (k < 0) continue;
     int a = e[2 * i], b = e[2 * i + 1];
-    val[start[key[i]] + slot[i]] = max(a, b);
+    val[start[k] + slot[i]] = max(a, b);
   }
 }
 
-// per bucket: insertion sort + unique in place, ucnt[v] = unique count
+// buckets up to kUeSmall entries: one thread, insertion sort + unique in
+// place, ucnt[v] = unique count.  Larger buckets are left to k_ue_sort_big.
+constexpr int kUeSmall = 32;
 __global__ void k_ue_sort(int64_t n, const int32_t *start, int32_t *val,
                           int32_t *ucnt) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
        v += (int64_t)gridDim.x * blockDim.x) {
     int b = start[v], e = start[v + 1];
+    if (e - b > kUeSmall) continue;
     for (int i = b + 1; i < e; ++i) {
       int x = val[i], j = i - 1;
       while (j >= b && val[j] > x) {
@@ -119,6 +131,69 @@ __global__ void k_ue_sort(int64_t n, const int32_t *start, int32_t *val,
   }
 }
 
+// Buckets above kUeSmall entries (hub vertices): a block per bucket, bottom-up
+// merge sort in which every element finds its merged position by a binary
+// search in the other run, ping-ponging between val[b, e) and the same range
+// of tmp (the per-edge slot array, free once k_ue_scatter has run).  Each
+// block scans kUeBigSpan consecutive buckets for large ones.
+constexpr int kUeBigSpan = 256;
+__global__ void k_ue_sort_big(int64_t n, const int32_t *start, int32_t *val,
+                              int32_t *tmp, int32_t *ucnt) {
+  __shared__ int32_t big[kUeBigSpan];
+  __shared__ int nbig;
+  const int64_t v0 = (int64_t)blockIdx.x * kUeBigSpan;
+  if (threadIdx.x == 0) nbig = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < kUeBigSpan; k += blockDim.x) {
+    int64_t v = v0 + k;
+    if (v < n && start[v + 1] - start[v] > kUeSmall) big[atomicAdd(&nbig, 1)] = (int32_t)v;
+  }
+  __syncthreads();
+  for (int q = 0; q < nbig; ++q) {
+    const int v = big[q];
+    const int b = start[v], s = start[v + 1] - b;
+    int32_t *src = val + b, *dst = tmp + b;
+    for (int w = 1; w < s; w *= 2) {
+      for (int i = threadIdx.x; i < s; i += blockDim.x) {
+        const int lo = (i / (2 * w)) * (2 * w);
+        const int mid = min(lo + w, s), hi = min(lo + 2 * w, s);
+        const int x = src[i];
+        int pos;
+        if (i < mid) {  // left run: count right-run elements < x
+          int l = mid, r = hi;
+          while (l < r) {
+            int m = (l + r) >> 1;
+            if (src[m] < x) l = m + 1; else r = m;
+          }
+          pos = lo + (i - lo) + (l - mid);
+        } else {        // right run: count left-run elements <= x
+          int l = lo, r = mid;
+          while (l < r) {
+            int m = (l + r) >> 1;
+            if (src[m] <= x) l = m + 1; else r = m;
+          }
+          pos = lo + (i - mid) + (l - lo);
+        }
+        dst[pos] = x;
+      }
+      __syncthreads();
+      int32_t *t = src;
+      src = dst;
+      dst = t;
+    }
+    if (src != val + b)
+      for (int i = threadIdx.x; i < s; i += blockDim.x) val[b + i] = src[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int u = 0;
+      for (int i = b; i < b + s; ++i)
+        if (i == b || val[i] != val[i - 1]) val[b + u++] = val[i];
+      ucnt[v] = u;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_ue_write(int64_t n, const int32_t *start, const int32_t *val,
                            const int32_t *ustart, int32_t *out) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
@@ -131,11 +206,12 @@ __global__ void k_ue_write(int64_t n, const int32_t *start, const int32_t *val,
   }
 }
 
+// cnt carries one extra slot, cnt[n], the bad-index flag
 static size_t carve_ue(Carve &c, int64_t n, int64_t m, int32_t **cnt,
                        int32_t **start, int32_t **key, int32_t **slot,
                        int32_t **val, int32_t **ucnt, int32_t **ustart,
                        int32_t **tmp) {
-  *cnt = c.take<int32_t>(n);
+  *cnt = c.take<int32_t>(n + 1);
   *start = c.take<int32_t>(n + 1);
   *key = c.take<int32_t>(m);
   *slot = c.take<int32_t>(m);
@@ -144,6 +220,38 @@ static size_t carve_ue(Carve &c, int64_t n, int64_t m, int32_t **cnt,
   *ustart = c.take<int32_t>(n + 1);
   *tmp = c.take<int32_t>(scan_tmp_elems(n));
   return c.used;
+}
+
+// the kernel sequence shared by both entry points, on carved arrays
+static int unique_edges_run(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
+                            int64_t *n_out, int32_t *cnt, int32_t *start, int32_t *key,
+                            int32_t *slot, int32_t *val, int32_t *ucnt, int32_t *ustart,
+                            int32_t *tmp, const char *who, cudaStream_t s) {
+  int32_t *bad = cnt + n;
+  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (n + 1), s));
+  int nb = grid_for(m, 256);
+  k_ue_count<<<nb, 256, 0, s>>>(edges, m, n, cnt, key, slot, bad);
+  int rc = exclusive_scan_i32(cnt, start, n, tmp, s);
+  if (rc) return rc;
+  k_ue_scatter<<<nb, 256, 0, s>>>(edges, m, start, key, slot, val);
+  k_ue_sort<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ucnt);
+  k_ue_sort_big<<<(int)((n + kUeBigSpan - 1) / kUeBigSpan), 256, 0, s>>>(n, start, val,
+                                                                         slot, ucnt);
+  rc = exclusive_scan_i32(ucnt, ustart, n, tmp, s);
+  if (rc) return rc;
+  k_ue_write<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ustart, out);
+  DM_LAUNCH_CHECK();
+  int32_t total = 0, flag = 0;
+  DM_CUDA_TRY(cudaMemcpyAsync(&total, ustart + n, sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaMemcpyAsync(&flag, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  DM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (flag) {
+    set_error("%s: an edge index lies outside [0, n = %lld)", who, (long long)n);
+    return DM_ERR_ARG;
+  }
+  *n_out = total;
+  return DM_OK;
 }
 
 int unique_edges_workspace(int64_t n, int64_t m, size_t *bytes) {
@@ -166,23 +274,8 @@ int unique_edges(const int32_t *edges, int64_t m, int64_t n, int32_t *out,
   }
   *n_out = 0;
   if (m == 0 || n == 0) return DM_OK;
-  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
-  int nb = grid_for(m, 256);
-  k_ue_count<<<nb, 256, 0, s>>>(edges, m, cnt, key, slot);
-  int rc = exclusive_scan_i32(cnt, start, n, tmp, s);
-  if (rc) return rc;
-  k_ue_scatter<<<nb, 256, 0, s>>>(edges, m, start, key, slot, val);
-  k_ue_sort<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ucnt);
-  rc = exclusive_scan_i32(ucnt, ustart, n, tmp, s);
-  if (rc) return rc;
-  k_ue_write<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ustart, out);
-  DM_LAUNCH_CHECK();
-  int32_t total = 0;
-  DM_CUDA_TRY(cudaMemcpyAsync(&total, ustart + n, sizeof(int32_t),
-                              cudaMemcpyDeviceToHost, s));
-  DM_CUDA_TRY(cudaStreamSynchronize(s));
-  *n_out = total;
-  return DM_OK;
+  return unique_edges_run(edges, m, n, out, n_out, cnt, start, key, slot, val, ucnt,
+                          ustart, tmp, "unique_edges", s);
 }
 
 // ---------------------------------------------------------------------------
@@ -252,23 +345,8 @@ int unique_edges_noalloc(const int32_t *edges, int64_t m, int64_t n,
   }
   *n_out = 0;
   if (m == 0 || n == 0) return DM_OK;
-  DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
-  int nb = grid_for(m, 256);
-  k_ue_count<<<nb, 256, 0, s>>>(edges, m, cnt, key, slot);
-  rc = exclusive_scan_i32(cnt, start, n, tmp, s);
-  if (rc) return rc;
-  k_ue_scatter<<<nb, 256, 0, s>>>(edges, m, start, key, slot, val);
-  k_ue_sort<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ucnt);
-  rc = exclusive_scan_i32(ucnt, ustart, n, tmp, s);
-  if (rc) return rc;
-  k_ue_write<<<grid_for(n, 128), 128, 0, s>>>(n, start, val, ustart, out);
-  DM_LAUNCH_CHECK();
-  int32_t total = 0;
-  DM_CUDA_TRY(cudaMemcpyAsync(&total, ustart + n, sizeof(int32_t),
-                              cudaMemcpyDeviceToHost, s));
-  DM_CUDA_TRY(cudaStreamSynchronize(s));
-  *n_out = total;
-  return DM_OK;
+  return unique_edges_run(edges, m, n, out, n_out, cnt, start, key, slot, val, ucnt,
+                          ustart, tmp, "unique_edges_noalloc", s);
 }
 
 }  // namespace dm

@@ -235,24 +235,31 @@ int compact_vertices(int dim, const float *P, float *Pout, int64_t n,
 // simplex signed volume and simp_qual (2 * inradius / circumradius of the
 // triangle formed by the first three vertices)
 template <int DIM>
-__global__ void k_simplex_metrics(const float *P, const int32_t *cells,
+__device__ __forceinline__ void load_vertex(const float *P, int64_t v, double *x) {
+  if (DIM == 3) {
+    float4 q = reinterpret_cast<const float4 *>(P)[v];
+    x[0] = q.x;
+    x[1] = q.y;
+    x[2] = q.z;
+  } else {
+    float2 q = reinterpret_cast<const float2 *>(P)[v];
+    x[0] = q.x;
+    x[1] = q.y;
+  }
+}
+// caller FP64 points: DIM doubles per row
+template <int DIM>
+__device__ __forceinline__ void load_vertex(const double *X, int64_t v, double *x) {
+  for (int d = 0; d < DIM; ++d) x[d] = X[v * DIM + d];
+}
+
+template <int DIM, typename PT>
+__global__ void k_simplex_metrics(const PT *P, const int32_t *cells,
                                   int64_t nc, double *vol, double *qual) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
        c += (int64_t)gridDim.x * blockDim.x) {
     double x[4][3] = {};
-    for (int k = 0; k <= DIM; ++k) {
-      int v = cells[(DIM + 1) * c + k];
-      if (DIM == 3) {
-        float4 q = reinterpret_cast<const float4 *>(P)[v];
-        x[k][0] = q.x;
-        x[k][1] = q.y;
-        x[k][2] = q.z;
-      } else {
-        float2 q = reinterpret_cast<const float2 *>(P)[v];
-        x[k][0] = q.x;
-        x[k][1] = q.y;
-      }
-    }
+    for (int k = 0; k <= DIM; ++k) load_vertex<DIM>(P, cells[(DIM + 1) * c + k], x[k]);
     if (vol) {
       double d1[3], d2[3], d3[3];
       for (int j = 0; j < 3; ++j) {
@@ -345,16 +352,27 @@ int re_ratios(int dim, const double *P, const int32_t *cells, int64_t nc, double
   return DM_OK;
 }
 
-int simplex_metrics(int dim, const float *P, const int32_t *cells, int64_t nc,
-                    double *vol, double *qual, cudaStream_t s) {
+template <typename PT>
+static int simplex_metrics_t(int dim, const PT *P, const int32_t *cells, int64_t nc,
+                             double *vol, double *qual, cudaStream_t s) {
   DM_ARG_CHECK(dim == 2 || dim == 3, "dim");
   if (nc == 0) return DM_OK;
   if (dim == 3)
-    k_simplex_metrics<3><<<grid_for(nc, 256), 256, 0, s>>>(P, cells, nc, vol, qual);
+    k_simplex_metrics<3, PT><<<grid_for(nc, 256), 256, 0, s>>>(P, cells, nc, vol, qual);
   else
-    k_simplex_metrics<2><<<grid_for(nc, 256), 256, 0, s>>>(P, cells, nc, vol, qual);
+    k_simplex_metrics<2, PT><<<grid_for(nc, 256), 256, 0, s>>>(P, cells, nc, vol, qual);
   DM_LAUNCH_CHECK();
   return DM_OK;
+}
+
+int simplex_metrics(int dim, const float *P, const int32_t *cells, int64_t nc,
+                    double *vol, double *qual, cudaStream_t s) {
+  return simplex_metrics_t(dim, P, cells, nc, vol, qual, s);
+}
+
+int simplex_metrics_f64(int dim, const double *X, const int32_t *cells, int64_t nc,
+                        double *vol, double *qual, cudaStream_t s) {
+  return simplex_metrics_t(dim, X, cells, nc, vol, qual, s);
 }
 
 }  // namespace dm

@@ -423,6 +423,15 @@ class _Engine:
 
         gu._laplacian_device(self)
 
+    def load_mesh(self, p, t):
+        """replace points and kept cells by a host mesh (p exact in float32:
+        it came from this engine's points)"""
+        self.set_points(D.to_points(p, self.dim))
+        nk = len(t)
+        if nk:
+            self.kept[:nk] = torch.from_numpy(np.ascontiguousarray(t, dtype=np.int32)).to(D.device())
+        self.counters[N.CNT_KEPT] = nk
+
     def result(self):
         nk = int(self.counters[N.CNT_KEPT].item())
         p = D.from_points(self.P, self.dim)
@@ -553,6 +562,12 @@ def _termination(eng, fd, opts, h0, deps, sliver=False):
         if opts["subdomains"] is None and opts["mesh_improvement"]:
             eng.laplacian_smooth()
     eng.compact()
+    if opts.get("perform_checks"):
+        # geometry.linter, as the reference's _termination does when asked
+        # (generation/mesh_generator.py:672-673)
+        p, t = eng.result()
+        p, t = geometry.linter(p, t, dim=eng.dim)
+        eng.load_mesh(p, t)
     if sliver:
         return
     eng.improve_level_set(fd, deps)

@@ -21,16 +21,22 @@ def _counter_block(n_cells, index=N.CNT_KEPT):
     return c
 
 
+def _points_f64(p, dim):
+    """caller points as a device float64 [n, dim] array (no narrowing: the
+    reference's drop-ins compute in FP64 on FP64 inputs)"""
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(p)[:, :dim], dtype=np.float64)).to(D.device())
+
+
 def simp_vol(p, t):
-    """Signed volumes of the simplices (geometry/utils.py:175-201)."""
+    """Signed volumes of the simplices (geometry/utils.py:175-201), FP64."""
     p = np.asarray(p)
     dim = p.shape[1]
     if len(t) == 0:
         return np.zeros(0)
-    P = D.to_points(p, dim)
+    X = _points_f64(p, dim)
     T = _cells_dev(t)
     vol = D.empty((len(t),), torch.float64)
-    N.call("dm_simplex_metrics", dim, D.ptr(P), D.ptr(T), len(t), D.ptr(vol), None, D.stream_ptr())
+    N.call("dm_simplex_metrics_f64", dim, D.ptr(X), D.ptr(T), len(t), D.ptr(vol), None, D.stream_ptr())
     return vol.cpu().numpy()
 
 
@@ -52,27 +58,27 @@ def calc_re_ratios(vertices, entities, dim=2):
 
 def simp_qual(p, t):
     """Radius-ratio quality 2 r / R of the triangle of the first three vertices
-    of each simplex (geometry/utils.py:252-274)."""
+    of each simplex (geometry/utils.py:252-274), FP64."""
     p = np.asarray(p)
     assert p.ndim == 2 and t.ndim == 2 and p.shape[1] + 1 == t.shape[1]
     dim = p.shape[1]
     if len(t) == 0:
         return np.zeros(0)
-    P = D.to_points(p, dim)
+    X = _points_f64(p, dim)
     T = _cells_dev(t)
     q = D.empty((len(t),), torch.float64)
-    N.call("dm_simplex_metrics", dim, D.ptr(P), D.ptr(T), len(t), None, D.ptr(q), D.stream_ptr())
+    N.call("dm_simplex_metrics_f64", dim, D.ptr(X), D.ptr(T), len(t), None, D.ptr(q), D.stream_ptr())
     return q.cpu().numpy()
 
 
 def calc_dihedral_angles(p, t):
     """6 dihedral angles per tetrahedron, shape (6 T, 1)
-    (geometry/cpp/fast_geometry.cpp:351-418)."""
-    P = D.to_points(np.asarray(p), 3)
+    (geometry/cpp/fast_geometry.cpp:351-418), FP64."""
+    X = _points_f64(p, 3)
     T = _cells_dev(t)
     out = D.empty((6 * len(t),), torch.float64)
     if len(t):
-        N.call("dm_dihedral_angles", D.ptr(P), D.ptr(T), len(t), D.ptr(out), D.stream_ptr())
+        N.call("dm_dihedral_angles_f64", D.ptr(X), D.ptr(T), len(t), D.ptr(out), D.stream_ptr())
     return out.cpu().numpy().reshape(-1, 1)
 
 
@@ -90,11 +96,14 @@ def calc_circumsphere_grad(p0, p1, p2, p3):
 
 
 def unique_edges(edges):
-    """Sorted unique (min, max) pairs (geometry/cpp/fast_geometry.cpp:30-77)."""
+    """Sorted unique (min, max) pairs (geometry/cpp/fast_geometry.cpp:30-77).
+    Vertex indices must be non-negative (they index the mesh's vertices)."""
     e = np.ascontiguousarray(np.asarray(edges, dtype=np.int32).reshape(-1, 2))
     m = e.shape[0]
     if m == 0:
         return np.zeros((0, 2), dtype=np.int32)
+    if int(e.min()) < 0:
+        raise ValueError("unique_edges: negative vertex index %d" % int(e.min()))
     n = int(e.max()) + 1
     E = torch.from_numpy(e).to(D.device())
     out = D.empty((m, 2), torch.int32)

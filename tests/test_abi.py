@@ -26,6 +26,34 @@ def test_library_loads_and_exports_every_declared_symbol():
     assert L.dm_version() >= 10000
 
 
+def test_diagnostic_header_matches_exports():
+    """every dmdbg_* / dmprof_* export is declared in include/dmgb_diag.h and
+    every declaration there is exported"""
+    src = open(os.path.join(ROOT, "include", "dmgb_diag.h")).read()
+    names = set(re.findall(r"^(?:int|int64_t)\s+(dm(?:dbg|prof)_\w+)\(", src, re.M))
+    L = N.lib()
+    assert len(names) >= 10
+    for name in names:
+        assert hasattr(L, name), name
+    import subprocess
+
+    from seismicmesh_gb300 import _build
+
+    out = subprocess.run(["nm", "-D", "--defined-only", _build.library_path()], capture_output=True, text=True)
+    if out.returncode == 0:
+        exported = set(re.findall(r"\b(dm(?:dbg|prof)_\w+)\b", out.stdout))
+        assert exported == names, exported ^ names
+
+
+def test_unique_edges_rejects_negative_indices_before_device_work():
+    import pytest
+
+    from seismicmesh_gb300 import geometry
+
+    with pytest.raises(ValueError, match="negative"):
+        geometry.unique_edges(np.array([[0, 1], [-1, 2]], dtype=np.int32))
+
+
 def test_error_reporting_on_bad_arguments():
     L = N.lib()
     nbytes = N.c_sz(0)
