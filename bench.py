@@ -17,8 +17,8 @@ Workload: 3D unit ball (Ball((0,0,0), 1)), constant edge length h = 0.02,
           generate_mesh; time_to_mesh_s includes sliver_removal.
 
 --impl reference times the reference's CPU loop (the oracle's float64 numpy
-restatement with Qhull connectivity; CGAL and MPI are not available) on a
-bounded sample of the workload, the same ball at h = 0.04 (66,394 points).
+restatement with Qhull connectivity; CGAL and MPI are not available) on the
+same workload: the h = 0.02 ball, one DistMesh iteration per step.
 With torchrun (N > 1) every rank meshes its own replica; value is the sum
 over ranks (timed with a barrier and the max over ranks).
 """
@@ -37,7 +37,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 H = 0.02
-SAMPLE_H = 0.04
 METRIC = "point-iterations/s (3D unit ball, h=0.02, DistMesh iterations)"
 
 
@@ -136,29 +135,65 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(steps, warmup):
-    """the oracle's restatement of the reference loop on the h = 0.04 ball"""
+def host_info():
+    """core count and CPU model of this host"""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k = line.split(":")[0].strip().lower()
+                if k in ("model name", "cpu part", "processor name"):
+                    model = line.split(":", 1)[1].strip()
+                    if k == "model name":
+                        break
+    except OSError:
+        pass
+    try:
+        lscpu = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in lscpu.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model}
+
+
+def cpu_sample(steps, warmup, h=H):
+    """the oracle's restatement of the reference loop (float64 numpy, Qhull
+    connectivity) on the unit ball at edge length h: `warmup` untimed
+    iterations from the initial lattice, then `steps` timed ones; returns
+    (points, seconds, per-step seconds)"""
     from oracle import distmesh_np as O
     from oracle import sdf_np as S
 
     fd = S.ball(0.0, 0.0, 0.0, 1.0)
-    fh = lambda x: np.full(len(x), SAMPLE_H)  # noqa: E731
+    fh = lambda x: np.full(len(x), h)  # noqa: E731
     bbox = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
-    p = O.initial_points(fd, fh, SAMPLE_H, bbox, 0.1 * SAMPLE_H, 3)
+    p = O.initial_points(fd, fh, h, bbox, 0.1 * h, 3)
     for _ in range(warmup):
-        p, _, _ = O.one_iteration(p, fd, fh, SAMPLE_H)
-    t0 = time.perf_counter()
+        p, _, _ = O.one_iteration(p, fd, fh, h)
+    per = []
     for _ in range(steps):
-        p, _, _ = O.one_iteration(p, fd, fh, SAMPLE_H)
-    dt = time.perf_counter() - t0
-    return len(p), dt
+        t0 = time.perf_counter()
+        p, _, _ = O.one_iteration(p, fd, fh, h)
+        per.append(time.perf_counter() - t0)
+    return len(p), sum(per), per
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU loop on this arm's workload: the h = 0.02 unit ball
+    (526,727 points), one DistMesh iteration per step, W untimed warm-up
+    iterations from the initial lattice, then K timed.  The reference package
+    itself cannot be installed on this machine (CGAL, Boost, GMP/MPFR and
+    mpi4py are absent), so its loop runs as the oracle's float64 numpy
+    restatement with Qhull connectivity; serial, as the reference's serial
+    mode is (its MPI mode is not runnable here)."""
     if rank != 0:
         return
-    n, dt = cpu_sample(args.steps, args.warmup)
+    n, dt, per = cpu_sample(args.steps, args.warmup)
     value = n * args.steps / dt
+    info = host_info()
     line = {
         "metric": METRIC,
         "value": value,
@@ -173,13 +208,20 @@ def run_reference(args, world, rank):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (initial lattice of the unit ball, seeded decimation)",
-        "config": {"workload": "3D unit ball h=0.04 sample of the h=0.02 ball (66,394 points), "
-                               "one DistMesh iteration per step", "n_points": n},
+        "config": {
+            "workload": "3D unit ball, h=0.02, DistMesh iterations after 'warmup' iterations from "
+                        "the initial lattice",
+            "n_points": n,
+            "parallelism": "serial (1 core)",
+        },
+        "host": info,
+        "phases_ms": {"step_ms_min": 1000 * min(per), "step_ms_max": 1000 * max(per)},
         "cpu_baseline": {
             "value": value, "unit": "point-iterations/s", "cores": 1, "kind": "port",
-            "sample": f"{args.steps} DistMesh iterations of the h=0.04 unit ball ({n} points), "
-                      "float64 numpy restatement of the reference loop, Qhull connectivity "
-                      "(CGAL not installable), serial",
+            "sample": f"{args.steps} DistMesh iterations of the h=0.02 unit ball ({n} points) after "
+                      f"{args.warmup} warm-up iterations: float64 numpy restatement of the reference "
+                      "loop with Qhull connectivity (CGAL not installable), serial; "
+                      f"host {info['nproc']} cores, {info['cpu_model']}",
         },
         "e2e": {"value": value, "unit": "point-iterations/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -358,11 +400,13 @@ def run_ours(args, world, rank, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        ncpu, dt = cpu_sample(2, 0)
+        ncpu, dt, _ = cpu_sample(1, 0)
+        info = host_info()
         cpu = {
-            "value": ncpu * 2 / dt, "unit": "point-iterations/s", "cores": 1, "kind": "port",
-            "sample": f"2 DistMesh iterations of the h=0.04 unit ball ({ncpu} points), float64 numpy "
-                      "restatement of the reference loop with Qhull connectivity, serial",
+            "value": ncpu / dt, "unit": "point-iterations/s", "cores": 1, "kind": "port",
+            "sample": f"1 DistMesh iteration of the h=0.02 unit ball ({ncpu} points) from the initial "
+                      "lattice: float64 numpy restatement of the reference loop with Qhull "
+                      f"connectivity, serial; host {info['nproc']} cores, {info['cpu_model']}",
         }
     if rank == 0:
         line = {

@@ -385,6 +385,128 @@ int dm_laplacian_smooth(float *points, int64_t n, const int32_t *adj,
                         double rtol, int32_t *iters_host, void *workspace,
                         size_t workspace_bytes, void *stream);
 
+/* ---- isosurface SDF of a gridded field (salt bodies) ---------------------
+ * No counterpart in the reference: its domains are analytic primitives and
+ * their CSG (geometry/signed_distance_functions.py:307-593).  This is the
+ * domain of a body given by a gridded field B (e.g. a salt indicator derived
+ * from a velocity model): inside where the piecewise-linear interpolant of B
+ * over the Kuhn split of every grid cell (6 tetrahedra along the cell's main
+ * diagonal) is >= level.  The surface is extracted by marching tetrahedra;
+ * dm_iso_eval returns the exact signed distance to it (negative inside) and
+ * its gradient.  All pointers in the struct are device pointers. */
+typedef struct dm_iso {
+  const float *field;    /* B at the nodes, float[n0][n1][n2], C order      */
+  float level;
+  int32_t n[3];          /* nodes per axis (>= 2)                           */
+  float origin[3];       /* node (0,0,0)                                    */
+  float h[3];            /* node spacing                                    */
+  const float *tris;     /* float[ntri][3][4]: vertices (x, y, z, 0)        */
+  int64_t ntri;
+  const int32_t *bstart; /* [nb0*nb1*nb2 + 1] triangles by box (CSR)        */
+  const int32_t *btri;   /* [ntri] triangle ids, ascending within a box     */
+  const int32_t *bring;  /* [nb] Chebyshev ring of the nearest non-empty box*/
+  int32_t nb[3];         /* boxes per axis                                  */
+  float bsize[3];        /* box edge lengths (boxes start at origin)        */
+  float rho;             /* how far a triangle reaches out of its box       */
+} dm_iso;
+/* triangle count of the surface: rowstart int32[2*(n0-1)*(n1-1) + 1]
+ * receives the exclusive scan of the per-row counts in its first
+ * (n0-1)*(n1-1) + 1 entries; tmp holds >= (n0-1)*(n1-1)/1024 + 16 ints.
+ * Synchronises the stream. */
+int dm_iso_count(const dm_iso *iso, int32_t *rowstart, int32_t *tmp,
+                 int64_t *ntri_host, void *stream);
+/* the triangles, float[ntri][3][4], in a fixed order (row, cell, tet) */
+int dm_iso_emit(const dm_iso *iso, const int32_t *rowstart, float *tris,
+                void *stream);
+/* boxes of the triangles: fills bstart/btri/bring and iso->rho (host
+ * struct updated, stream synchronised); iso->tris, ntri, nb, bsize set by
+ * the caller */
+int dm_iso_bucket_workspace_size(int64_t ntri, int64_t n_boxes, size_t *bytes);
+int dm_iso_bucket(dm_iso *iso, int32_t *bstart, int32_t *btri, int32_t *bring,
+                  void *workspace, size_t workspace_bytes, void *stream);
+/* signed distance d[i] (and grad float[n][4], may be NULL) of the points
+ * float[n][stride]; with idx only the listed points are evaluated, and with
+ * count (device) their number is read on the device (n is then an upper
+ * bound used for the launch shape). */
+int dm_iso_eval(const dm_iso *iso, const float *points, int32_t stride,
+                int64_t n, const int32_t *idx, const int64_t *count,
+                float *d, float *grad, void *stream);
+
+/* ---- batched-SDF steps of the DistMesh loop --------------------------------
+ * The counterparts of dm_filter_cells and of the projection inside
+ * dm_update_points for domains whose distances are computed by a separate
+ * batched evaluation (dm_iso_eval, dm_mlp_eval) rather than an inline
+ * program: _remove_triangles_outside (generation/mesh_generator.py:734-738)
+ * keeps cell c when d[c] < -geps (cells_out, count in
+ * counters[DM_CNT_KEPT]); _project_points_back_newton (762-784) moves every
+ * point with d > 0 by -d grad (grad float[n][4], unit length, as the exact
+ * SDF returns), then rounds to the position grid as dm_update_points does. */
+int dm_filter_cells_by_value(int32_t dim, const int32_t *cells, int64_t cap_cells,
+                             const float *d, float geps, int32_t *cells_out,
+                             int64_t *counters, void *stream);
+int dm_project_by_value(int32_t dim, float *points, int64_t n, const float *d,
+                        const float *grad, int32_t grid_exp, void *stream);
+/* _improve_level_set_newton (generation/mesh_generator.py:741-759) step on
+ * the m listed points: p -= alpha d grad, rounded to the position grid */
+int dm_newton_by_value(int32_t dim, float *points, const int32_t *idx, int64_t m,
+                       const float *d, const float *grad, float alpha, int32_t grid_exp,
+                       void *stream);
+/* indices i < n with lo < d[i] < hi, appended to idx; *count (device) is
+ * set to their number */
+int dm_select_band(const float *d, int64_t n, float lo, float hi, int32_t *idx,
+                   int64_t *count, void *stream);
+
+/* ---- neural signed distance (Fourier-feature MLP) ------------------------
+ * No counterpart in the reference.  A learned stand-in for an expensive SDF
+ * (dm_iso): x_n = (x - center) * inv_scale; features sin(2 pi F x_n),
+ * cos(2 pi F x_n) for the 32 rows of F; 4 hidden layers of 128 (ReLU);
+ * d = out_scale * (w5 . h4 + b5).  Parameters are FP32 (training), with
+ * BF16 copies of W1..W4 for the tensor-core inference kernel.
+ * Parameter layout (DM_MLP_NPARAMS floats): W1[128][64] b1[128]
+ * W2[128][128] b2[128] W3[128][128] b3[128] W4[128][128] b4[128] w5[128]
+ * b5[1]. */
+#define DM_MLP_NFREQ 32
+#define DM_MLP_NFEAT 64
+#define DM_MLP_WIDTH 128
+#define DM_MLP_NPARAMS (128 * 64 + 128 + 3 * (128 * 128 + 128) + 128 + 1)
+#define DM_MLP_NBF16 (128 * 64 + 3 * 128 * 128)
+typedef struct dm_mlp {
+  float freq[DM_MLP_NFREQ * 3]; /* Fourier frequencies F[32][3] (host values) */
+  float center[3];
+  float inv_scale;
+  float out_scale;
+  const float *params;   /* device, DM_MLP_NPARAMS FP32                      */
+  const uint16_t *wbf16; /* device, DM_MLP_NBF16 BF16 (W1, W2, W3, W4)       */
+} dm_mlp;
+/* one training step's gradient: forward and backward of the batch x
+ * float[batch][4] against target float[batch] (in units of out_scale) with
+ * per-sample weights (may be NULL), loss = sum w (y - t)^2 / batch;
+ * grads float[DM_MLP_NPARAMS] (device) receives d loss / d params and
+ * loss_dev (device, may be NULL) the loss.  FP32 throughout. */
+int dm_mlp_train_workspace_size(int64_t batch, size_t *bytes);
+int dm_mlp_forward_backward(const dm_mlp *mlp, const float *x, const float *target,
+                            const float *weight, int64_t batch, float *grads,
+                            float *loss_dev, void *workspace, size_t workspace_bytes,
+                            void *stream);
+/* Adam (Kingma & Ba 2015) on n parameters, step t >= 1 */
+int dm_mlp_adam(float *params, const float *grads, float *m1, float *m2, int64_t n,
+                float lr, float beta1, float beta2, float eps, int32_t t, void *stream);
+/* BF16 copies of W1..W4 (round to nearest even) */
+int dm_mlp_to_bf16(const float *params, uint16_t *wbf16, void *stream);
+/* FP32 forward (the training path's arithmetic): d[i] for points
+ * float[n][stride] */
+int dm_mlp_eval_fp32(const dm_mlp *mlp, const float *points, int32_t stride, int64_t n,
+                     float *d, void *workspace, size_t workspace_bytes, void *stream);
+/* inference on the 5th-generation tensor cores: BF16 weights and
+ * activations, FP32 accumulation in tensor memory (tcgen05.mma, weights
+ * staged by TMA); one persistent CTA per SM.  d[i] for points
+ * float[n][stride].  Every wait inside the kernel gives up after 2 s and
+ * records it; dm_mlp_eval_status (synchronises the stream) returns 1 in
+ * *timed_out_host when that happened since the last status call. */
+int dm_mlp_eval(const dm_mlp *mlp, const float *points, int32_t stride, int64_t n,
+                float *d, void *stream);
+int dm_mlp_eval_status(int32_t *timed_out_host, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

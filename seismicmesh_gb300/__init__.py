@@ -3,7 +3,7 @@
 generate_mesh / sliver_removal, the SDF classes and the sizing calls run on
 hand-written sm_103a CUDA kernels (libdmgb.so, C ABI in include/dmgb.h).
 """
-from . import geometry, sizing
+from . import geometry, sizing, synthetic
 from .generation import generate_mesh, sliver_removal
 from .geometry import (
     Ball,
@@ -13,6 +13,8 @@ from .geometry import (
     Disk,
     GridSDF,
     Intersection,
+    Isosurface,
+    NeuralSDF,
     Prism,
     Rectangle,
     Repeat,
@@ -33,5 +35,6 @@ __all__ = [
     "generate_mesh", "sliver_removal", "geometry", "sizing", "Ball", "Cube", "Cylinder",
     "Difference", "Disk", "GridSDF", "Intersection", "Prism", "Rectangle", "Repeat",
     "Torus", "Union", "SizeFunction", "get_sizing_function_from_segy",
-    "plot_sizing_function", "read_velocity_model", "write_velocity_model",
+    "plot_sizing_function", "read_velocity_model", "write_velocity_model", "Isosurface",
+    "NeuralSDF", "synthetic",
 ]

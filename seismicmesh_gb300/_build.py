@@ -19,6 +19,8 @@ SOURCES = [
     "dm_mesh.cu",
     "dm_sizing.cu",
     "dm_topo.cu",
+    "dm_iso.cu",
+    "dm_mlp.cu",
     "dm_capi.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

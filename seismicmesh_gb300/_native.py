@@ -60,6 +60,42 @@ class Sizing(ctypes.Structure):
     ]
 
 
+class Iso(ctypes.Structure):
+    """dm_iso: isosurface SDF of a gridded field (device pointers)"""
+    _fields_ = [
+        ("field", c_p),
+        ("level", c_f),
+        ("n", c_int * 3),
+        ("origin", c_f * 3),
+        ("h", c_f * 3),
+        ("tris", c_p),
+        ("ntri", c_i64),
+        ("bstart", c_p),
+        ("btri", c_p),
+        ("bring", c_p),
+        ("nb", c_int * 3),
+        ("bsize", c_f * 3),
+        ("rho", c_f),
+    ]
+
+
+MLP_NFREQ = 32
+MLP_NPARAMS = 128 * 64 + 128 + 3 * (128 * 128 + 128) + 128 + 1
+MLP_NBF16 = 128 * 64 + 3 * 128 * 128
+
+
+class Mlp(ctypes.Structure):
+    """dm_mlp: Fourier-feature MLP SDF (params / wbf16 are device pointers)"""
+    _fields_ = [
+        ("freq", c_f * (MLP_NFREQ * 3)),
+        ("center", c_f * 3),
+        ("inv_scale", c_f),
+        ("out_scale", c_f),
+        ("params", c_p),
+        ("wbf16", c_p),
+    ]
+
+
 _FP = ctypes.POINTER(c_f)
 
 # name -> (restype, argtypes)
@@ -137,6 +173,23 @@ SIGNATURES = {
          c_int, c_int, c_d, c_p, c_p],
     ),
     "dm_laplacian_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_iso_count": (c_int, [ctypes.POINTER(Iso), c_p, c_p, ctypes.POINTER(c_i64), c_p]),
+    "dm_iso_emit": (c_int, [ctypes.POINTER(Iso), c_p, c_p, c_p]),
+    "dm_iso_bucket_workspace_size": (c_int, [c_i64, c_i64, ctypes.POINTER(c_sz)]),
+    "dm_iso_bucket": (c_int, [ctypes.POINTER(Iso), c_p, c_p, c_p, c_p, c_sz, c_p]),
+    "dm_iso_eval": (c_int, [ctypes.POINTER(Iso), c_p, c_int, c_i64, c_p, c_p, c_p, c_p, c_p]),
+    "dm_filter_cells_by_value": (c_int, [c_int, c_p, c_i64, c_p, c_f, c_p, c_p, c_p]),
+    "dm_project_by_value": (c_int, [c_int, c_p, c_i64, c_p, c_p, c_int, c_p]),
+    "dm_select_band": (c_int, [c_p, c_i64, c_f, c_f, c_p, c_p, c_p]),
+    "dm_newton_by_value": (c_int, [c_int, c_p, c_p, c_i64, c_p, c_p, c_f, c_int, c_p]),
+    "dm_mlp_train_workspace_size": (c_int, [c_i64, ctypes.POINTER(c_sz)]),
+    "dm_mlp_forward_backward": (
+        c_int, [ctypes.POINTER(Mlp), c_p, c_p, c_p, c_i64, c_p, c_p, c_p, c_sz, c_p]),
+    "dm_mlp_adam": (c_int, [c_p, c_p, c_p, c_p, c_i64, c_f, c_f, c_f, c_f, c_int, c_p]),
+    "dm_mlp_to_bf16": (c_int, [c_p, c_p, c_p]),
+    "dm_mlp_eval_fp32": (c_int, [ctypes.POINTER(Mlp), c_p, c_int, c_i64, c_p, c_p, c_sz, c_p]),
+    "dm_mlp_eval": (c_int, [ctypes.POINTER(Mlp), c_p, c_int, c_i64, c_p, c_p]),
+    "dm_mlp_eval_status": (c_int, [ctypes.POINTER(c_int), c_p]),
     "dm_laplacian_smooth": (
         c_int,
         [c_p, c_i64, c_p, c_int, c_p, c_p, c_int, c_d, ctypes.POINTER(c_int), c_p, c_sz, c_p],

@@ -98,6 +98,33 @@ int laplacian_smooth(float *P, int64_t n, const int32_t *adj, int cap,
                      const int32_t *deg, const int32_t *bflag, int max_iter,
                      double rtol, int *iters_out, void *ws, size_t ws_bytes,
                      cudaStream_t s);
+int iso_count(const dm_iso *I, int32_t *rowstart, int32_t *tmp, int64_t *ntri, cudaStream_t s);
+int iso_emit(const dm_iso *I, const int32_t *rowstart, float *tris, cudaStream_t s);
+size_t iso_bucket_workspace(int64_t ntri, int64_t nbk);
+int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, void *ws,
+               size_t ws_bytes, cudaStream_t s);
+int iso_eval(const dm_iso *I, const float *pts, int stride, int64_t n, const int32_t *idx,
+             const int64_t *count_dev, float *d, float *grad, cudaStream_t s);
+int filter_by_value(int dim, const int32_t *cells, int64_t cap, const float *d, float geps,
+                    int32_t *out, int64_t *counters, cudaStream_t s);
+int project_by_value(int dim, float *P, int64_t n, const float *d, const float *grad,
+                     int grid_exp, cudaStream_t s);
+int select_band(const float *d, int64_t n, float lo, float hi, int32_t *idx, int64_t *count,
+                cudaStream_t s);
+int newton_by_value(int dim, float *P, const int32_t *idx, int64_t m, const float *d,
+                    const float *grad, float alpha, int grid_exp, cudaStream_t s);
+size_t mlp_train_workspace(int64_t batch);
+int mlp_forward_backward(const dm_mlp *m, const float *x, const float *target,
+                         const float *weight, int64_t batch, float *grads, float *loss,
+                         void *ws, size_t ws_bytes, cudaStream_t s);
+int mlp_adam(float *params, const float *grads, float *m1, float *m2, int64_t n, float lr,
+             float b1, float b2, float eps, int t, cudaStream_t s);
+int mlp_to_bf16(const float *params, uint16_t *w, cudaStream_t s);
+int mlp_eval_fp32(const dm_mlp *m, const float *pts, int stride, int64_t n, float *d,
+                  void *ws, size_t ws_bytes, cudaStream_t s);
+int mlp_eval_tc(const dm_mlp *m, const float *pts, int stride, int64_t n, float *d,
+                cudaStream_t s);
+int mlp_tc_status(cudaStream_t s, int *status);
 }  // namespace dm
 
 #define S(x) reinterpret_cast<cudaStream_t>(x)
@@ -106,7 +133,7 @@ extern "C" {
 
 int dm_version(void) { return 10000; }
 const char *dm_last_error(void) { return dm::last_error(); }
-int dm_abi_count(void) { return 47; }
+int dm_abi_count(void) { return 63; }
 
 int dm_orient2(const float *a, const float *b, const float *c) {
   dmp::ExactScratch W;
@@ -442,3 +469,74 @@ extern "C" int dmdbg_host_pred(int kind, const float *a, const float *b,
   }
   return -99;
 }
+
+// ---- isosurface SDF, batched-SDF steps, neural SDF -------------------------
+extern "C" {
+int dm_iso_count(const dm_iso *iso, int32_t *rowstart, int32_t *tmp, int64_t *ntri_host,
+                 void *stream) {
+  return dm::iso_count(iso, rowstart, tmp, ntri_host, S(stream));
+}
+int dm_iso_emit(const dm_iso *iso, const int32_t *rowstart, float *tris, void *stream) {
+  return dm::iso_emit(iso, rowstart, tris, S(stream));
+}
+int dm_iso_bucket_workspace_size(int64_t ntri, int64_t n_boxes, size_t *bytes) {
+  if (!bytes || ntri < 0 || n_boxes <= 0) return DM_ERR_ARG;
+  *bytes = dm::iso_bucket_workspace(ntri, n_boxes);
+  return DM_OK;
+}
+int dm_iso_bucket(dm_iso *iso, int32_t *bstart, int32_t *btri, int32_t *bring, void *workspace,
+                  size_t workspace_bytes, void *stream) {
+  return dm::iso_bucket(iso, bstart, btri, bring, workspace, workspace_bytes, S(stream));
+}
+int dm_iso_eval(const dm_iso *iso, const float *points, int32_t stride, int64_t n,
+                const int32_t *idx, const int64_t *count, float *d, float *grad, void *stream) {
+  return dm::iso_eval(iso, points, stride, n, idx, count, d, grad, S(stream));
+}
+int dm_filter_cells_by_value(int32_t dim, const int32_t *cells, int64_t cap_cells,
+                             const float *d, float geps, int32_t *cells_out,
+                             int64_t *counters, void *stream) {
+  return dm::filter_by_value(dim, cells, cap_cells, d, geps, cells_out, counters, S(stream));
+}
+int dm_project_by_value(int32_t dim, float *points, int64_t n, const float *d,
+                        const float *grad, int32_t grid_exp, void *stream) {
+  return dm::project_by_value(dim, points, n, d, grad, grid_exp, S(stream));
+}
+int dm_newton_by_value(int32_t dim, float *points, const int32_t *idx, int64_t m,
+                       const float *d, const float *grad, float alpha, int32_t grid_exp,
+                       void *stream) {
+  return dm::newton_by_value(dim, points, idx, m, d, grad, alpha, grid_exp, S(stream));
+}
+int dm_select_band(const float *d, int64_t n, float lo, float hi, int32_t *idx,
+                   int64_t *count, void *stream) {
+  return dm::select_band(d, n, lo, hi, idx, count, S(stream));
+}
+int dm_mlp_train_workspace_size(int64_t batch, size_t *bytes) {
+  if (!bytes || batch <= 0) return DM_ERR_ARG;
+  *bytes = dm::mlp_train_workspace(batch);
+  return DM_OK;
+}
+int dm_mlp_forward_backward(const dm_mlp *mlp, const float *x, const float *target,
+                            const float *weight, int64_t batch, float *grads, float *loss_dev,
+                            void *workspace, size_t workspace_bytes, void *stream) {
+  return dm::mlp_forward_backward(mlp, x, target, weight, batch, grads, loss_dev, workspace,
+                                  workspace_bytes, S(stream));
+}
+int dm_mlp_adam(float *params, const float *grads, float *m1, float *m2, int64_t n, float lr,
+                float beta1, float beta2, float eps, int32_t t, void *stream) {
+  return dm::mlp_adam(params, grads, m1, m2, n, lr, beta1, beta2, eps, t, S(stream));
+}
+int dm_mlp_to_bf16(const float *params, uint16_t *wbf16, void *stream) {
+  return dm::mlp_to_bf16(params, wbf16, S(stream));
+}
+int dm_mlp_eval_fp32(const dm_mlp *mlp, const float *points, int32_t stride, int64_t n,
+                     float *d, void *workspace, size_t workspace_bytes, void *stream) {
+  return dm::mlp_eval_fp32(mlp, points, stride, n, d, workspace, workspace_bytes, S(stream));
+}
+int dm_mlp_eval(const dm_mlp *mlp, const float *points, int32_t stride, int64_t n, float *d,
+                void *stream) {
+  return dm::mlp_eval_tc(mlp, points, stride, n, d, S(stream));
+}
+int dm_mlp_eval_status(int32_t *timed_out_host, void *stream) {
+  return dm::mlp_tc_status(S(stream), timed_out_host);
+}
+}  // extern "C"

@@ -66,9 +66,12 @@ class _Domain:
     def __init__(self, obj):
         self.obj = obj
         self.is_program = hasattr(obj, "device_program")
+        # distances from a separate batched device evaluation (Isosurface,
+        # NeuralSDF): no inline program, no host round trip
+        self.is_batched = hasattr(obj, "batched_eval")
 
     def __call__(self, x):
-        if self.is_program:
+        if self.is_program or self.is_batched:
             return self.obj.eval(x)
         return np.asarray(self.obj(x), dtype=float)
 
@@ -234,6 +237,21 @@ class _Engine:
         self.set_points(self.P[torch.from_numpy(keep).to(self.P.device)].contiguous())
 
     def filter(self, domain, geps):
+        if domain.is_batched:
+            # centroids, then their distances in one batched evaluation
+            nc = int(self.counters[N.CNT_CELLS].item())
+            cen = D.empty((max(nc, 1), self.dim), torch.float32)
+            N.call(
+                "dm_cell_centroids", self.dim, D.ptr(self.P), D.ptr(self.cells), self.cap_cells,
+                D.ptr(self.counters), D.ptr(cen), D.stream_ptr(),
+            )
+            d = D.empty((max(nc, 1),), torch.float32)
+            domain.obj.batched_eval(cen, self.dim, nc, d, mode="cells")
+            N.call(
+                "dm_filter_cells_by_value", self.dim, D.ptr(self.cells), nc, D.ptr(d), geps,
+                D.ptr(self.kept), D.ptr(self.counters), D.stream_ptr(),
+            )
+            return int(self.counters[N.CNT_KEPT].item())
         if domain.is_program:
             N.call(
                 "dm_filter_cells", self.dim, D.ptr(self.P), D.ptr(self.cells), self.cap_cells,
@@ -348,6 +366,16 @@ class _Engine:
         self.counters[N.CNT_KEPT] = nk
         return nk
 
+    def project_batched(self, domain):
+        """_project_points_back_newton with batched device distances: points
+        with d > 0 move by -d grad (the exact SDF's unit gradient)"""
+        d = D.empty((self.n,), torch.float32)
+        g = D.empty((self.n, 4), torch.float32)
+        W = self.P.shape[1]
+        domain.obj.batched_eval(self.P, W, self.n, d, g, mode="points")
+        N.call("dm_project_by_value", self.dim, D.ptr(self.P), self.n, D.ptr(d), D.ptr(g),
+               self.grid_exp, D.stream_ptr())
+
     def project_host(self, levels, deps, hmin):
         """Newton projection on the host, for runs with a host-callable level
         (the slow path: positions make one round trip per iteration)"""
@@ -359,6 +387,24 @@ class _Engine:
         self.P.copy_(D.to_points(p, self.dim))
 
     def improve_level_set(self, domain, deps):
+        if domain.is_batched:
+            # _improve_level_set_newton with exact distances and gradients at
+            # the boundary vertices: 5 damped steps p -= alpha d grad
+            bid = self.boundary_vertices(N.CNT_KEPT)
+            m = bid.numel()
+            if m == 0:
+                return
+            d = D.empty((self.n,), torch.float32)
+            g = D.empty((self.n, 4), torch.float32)
+            cnt = torch.tensor([m], dtype=torch.int64, device=self.P.device)
+            W = self.P.shape[1]
+            alpha = 1.0
+            for it in range(5):
+                domain.obj.batched_eval(self.P, W, self.n, d, g, idx=bid, count=cnt)
+                N.call("dm_newton_by_value", self.dim, D.ptr(self.P), D.ptr(bid), m, D.ptr(d),
+                       D.ptr(g), alpha, self.grid_exp, D.stream_ptr())
+                alpha /= it + 1
+            return
         if not domain.is_program:
             # _improve_level_set_newton (generation/mesh_generator.py:741-759)
             # with the host callable
@@ -522,8 +568,11 @@ def generate_mesh(domain, edge_length, comm=None, **kwargs):  # noqa: C901
         for sub in gen_opts["subdomains"]:
             sfd, _, _ = _unpack_domain(sub, gen_opts)
             levels.append(sfd)
+    batched = fd.is_batched
+    if batched and len(levels) > 1:
+        raise NotImplementedError("subdomains are not supported with a batched-SDF domain")
     # a host-callable level moves the projection to the host (slow path)
-    host_levels = not all(lv.is_program for lv in levels)
+    host_levels = not batched and not all(lv.is_program for lv in levels)
     if host_levels:
         print_msg1("Host-callable domain: the Newton projection runs on the host")
 
@@ -538,8 +587,10 @@ def generate_mesh(domain, edge_length, comm=None, **kwargs):  # noqa: C901
             _termination(eng, fd, gen_opts, h0, deps)
             break
         eng.build_adjacency()
-        eng.step(sizing, [] if host_levels else levels, L0mult, delta_t, h0, deps)
-        if host_levels:
+        eng.step(sizing, [] if (host_levels or batched) else levels, L0mult, delta_t, h0, deps)
+        if batched:
+            eng.project_batched(fd)
+        elif host_levels:
             eng.project_host(levels, deps, h0)
         maxdp = eng.max_movement(delta_t)
         print_msg2(
@@ -755,6 +806,9 @@ def _unpack_domain(domain, opts):
         bbox = domain.bbox
         fd = _Domain(domain)
         corners = domain.corners
+    elif hasattr(domain, "batched_eval"):
+        bbox = tuple(domain.bbox)
+        fd = _Domain(domain)
     elif callable(domain):
         bbox = opts["bbox"]
         fd = _Domain(domain)

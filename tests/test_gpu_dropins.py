@@ -2,7 +2,8 @@
 FP64 points (the reference computes in FP64, so do these entry points) and
 unique_edges with hub vertices whose buckets take the block merge sort.
 
-Tolerances: FP64 results within 1e-12 relative of the oracle's FP64 numpy
+Tolerances: FP64 results within 1e-12 relative (dihedral angles: or 1e-9 rad
+absolute) or 1e-10 relative (volumes, qualities) of the oracle's FP64 numpy
 restatement (pinned to the reference's outputs in test_oracle.py); integer
 pairs exact."""
 import numpy as np
@@ -28,7 +29,9 @@ def test_dihedral_angles_are_fp64_on_unrounded_points(cuda):
     assert not np.array_equal(p, p.astype(np.float32).astype(np.float64))
     got = sm.geometry.calc_dihedral_angles(p, t)
     ref = O.dihedral_angles(p, t)
-    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+    # acos is ill-conditioned near 0 and pi (flat hull tetrahedra of the
+    # random set): 1e-12 relative, and 1e-9 rad absolute there
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-9)
 
 
 def test_simp_vol_and_qual_are_fp64_on_unrounded_points(cuda):

@@ -22,9 +22,9 @@ pytestmark = pytest.mark.gpu
 RTOL = 1e-5
 
 
-def _one_iteration(p0, domain, h):
+def _one_iteration(p0, domain, h, grid=False):
     dim = p0.shape[1]
-    eng = MG._Engine(dim, p0, 0, grid=False)
+    eng = MG._Engine(dim, p0, 0, grid=grid)
     eng.triangulate()
     fd = MG._Domain(domain)
     eng.filter(fd, 0.1 * h)
@@ -43,10 +43,15 @@ def _one_iteration(p0, domain, h):
     ("iter_rect.npz", lambda: sm.Rectangle((0.0, 1.0, 0.0, 2.0))),
     ("iter_cube.npz", lambda: sm.Cube((0.0, 1.0, 0.0, 1.0, 0.0, 1.0))),
 ])
-def test_one_distmesh_iteration_matches_reference(cuda, name, shape):
+@pytest.mark.parametrize("grid", [False, True], ids=["float32", "position-grid"])
+def test_one_distmesh_iteration_matches_reference(cuda, name, shape, grid):
+    """grid=True is the production path: the points are snapped to the run's
+    position grid (a move of at most half a float32 ulp at the largest
+    coordinate), the predicates run in fixed point and the update rounds
+    back onto the grid; the same 1e-5 bound holds."""
     g = golden(name)
     h = float(g["h"])
-    p1, t = _one_iteration(g["p0"], shape(), h)
+    p1, t = _one_iteration(g["p0"], shape(), h, grid=grid)
     # connectivity of the kept cells: identical (generic points)
     np.testing.assert_array_equal(dc.canonical(t), dc.canonical(g["t"]))
     scale = np.abs(g["p1"]).max()
