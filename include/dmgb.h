@@ -408,6 +408,11 @@ typedef struct dm_iso {
   int32_t nb[3];         /* boxes per axis                                  */
   float bsize[3];        /* box edge lengths (boxes start at origin)        */
   float rho;             /* how far a triangle reaches out of its box       */
+  int32_t cf;            /* coarse level: blocks of cf^3 boxes (>= 1)       */
+  int32_t ncb[3];        /* blocks per axis: ceil(nb / cf)                  */
+  const int32_t *cocc;   /* [ncb] triangles in the block                    */
+  const int32_t *cring;  /* [ncb] Chebyshev ring of the nearest non-empty   */
+                         /* block                                           */
 } dm_iso;
 /* triangle count of the surface: rowstart int32[2*(n0-1)*(n1-1) + 1]
  * receives the exclusive scan of the per-row counts in its first
@@ -418,12 +423,15 @@ int dm_iso_count(const dm_iso *iso, int32_t *rowstart, int32_t *tmp,
 /* the triangles, float[ntri][3][4], in a fixed order (row, cell, tet) */
 int dm_iso_emit(const dm_iso *iso, const int32_t *rowstart, float *tris,
                 void *stream);
-/* boxes of the triangles: fills bstart/btri/bring and iso->rho (host
- * struct updated, stream synchronised); iso->tris, ntri, nb, bsize set by
- * the caller */
+/* boxes of the triangles: fills bstart/btri/bring, the coarse level
+ * (coarse: int32[2 * ncb0*ncb1*ncb2], occupancy then rings) and iso->rho
+ * (host struct updated, stream synchronised); iso->tris, ntri, nb, bsize,
+ * cf and ncb are set by the caller.  A query scans the rings of blocks
+ * around it and descends only into blocks holding triangles. */
 int dm_iso_bucket_workspace_size(int64_t ntri, int64_t n_boxes, size_t *bytes);
 int dm_iso_bucket(dm_iso *iso, int32_t *bstart, int32_t *btri, int32_t *bring,
-                  void *workspace, size_t workspace_bytes, void *stream);
+                  int32_t *coarse, void *workspace, size_t workspace_bytes,
+                  void *stream);
 /* signed distance d[i] (and grad float[n][4], may be NULL) of the points
  * float[n][stride]; with idx only the listed points are evaluated, and with
  * count (device) their number is read on the device (n is then an upper

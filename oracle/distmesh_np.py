@@ -325,3 +325,17 @@ def sliver_removal(p, fd, h0, max_iter=50, min_dh=10.0, max_dh=180.0, gamma=1.0,
         p[t[bad, 0]] += step * h0 * g
         old = nb
     return fix_mesh(p, t, delete_unused=True)
+
+
+def jittered_ball_points(h, seed=0):
+    """The reference's initial points of the unit ball at constant size h
+    (initial_points: lattice, rejection, decimation) moved by a seeded
+    U(-1e-3 h, 1e-3 h) per coordinate and rounded to float32: a generic
+    start, where every Delaunay triangulation of the run is unique."""
+    from . import sdf_np as S
+
+    fd = S.ball(0.0, 0.0, 0.0, 1.0)
+    p0 = initial_points(fd, lambda x: np.full(len(x), h), h, (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0),
+                        0.1 * h, 3)
+    rng = np.random.default_rng(seed)
+    return (p0 + rng.uniform(-1e-3 * h, 1e-3 * h, p0.shape)).astype(np.float32).astype(np.float64)

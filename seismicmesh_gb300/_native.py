@@ -76,6 +76,10 @@ class Iso(ctypes.Structure):
         ("nb", c_int * 3),
         ("bsize", c_f * 3),
         ("rho", c_f),
+        ("cf", c_int),
+        ("ncb", c_int * 3),
+        ("cocc", c_p),
+        ("cring", c_p),
     ]
 
 
@@ -176,7 +180,7 @@ SIGNATURES = {
     "dm_iso_count": (c_int, [ctypes.POINTER(Iso), c_p, c_p, ctypes.POINTER(c_i64), c_p]),
     "dm_iso_emit": (c_int, [ctypes.POINTER(Iso), c_p, c_p, c_p]),
     "dm_iso_bucket_workspace_size": (c_int, [c_i64, c_i64, ctypes.POINTER(c_sz)]),
-    "dm_iso_bucket": (c_int, [ctypes.POINTER(Iso), c_p, c_p, c_p, c_p, c_sz, c_p]),
+    "dm_iso_bucket": (c_int, [ctypes.POINTER(Iso), c_p, c_p, c_p, c_p, c_p, c_sz, c_p]),
     "dm_iso_eval": (c_int, [ctypes.POINTER(Iso), c_p, c_int, c_i64, c_p, c_p, c_p, c_p, c_p]),
     "dm_filter_cells_by_value": (c_int, [c_int, c_p, c_i64, c_p, c_f, c_p, c_p, c_p]),
     "dm_project_by_value": (c_int, [c_int, c_p, c_i64, c_p, c_p, c_int, c_p]),

@@ -101,8 +101,8 @@ int laplacian_smooth(float *P, int64_t n, const int32_t *adj, int cap,
 int iso_count(const dm_iso *I, int32_t *rowstart, int32_t *tmp, int64_t *ntri, cudaStream_t s);
 int iso_emit(const dm_iso *I, const int32_t *rowstart, float *tris, cudaStream_t s);
 size_t iso_bucket_workspace(int64_t ntri, int64_t nbk);
-int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, void *ws,
-               size_t ws_bytes, cudaStream_t s);
+int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, int32_t *coarse,
+               void *ws, size_t ws_bytes, cudaStream_t s);
 int iso_eval(const dm_iso *I, const float *pts, int stride, int64_t n, const int32_t *idx,
              const int64_t *count_dev, float *d, float *grad, cudaStream_t s);
 int filter_by_value(int dim, const int32_t *cells, int64_t cap, const float *d, float geps,
@@ -484,9 +484,9 @@ int dm_iso_bucket_workspace_size(int64_t ntri, int64_t n_boxes, size_t *bytes) {
   *bytes = dm::iso_bucket_workspace(ntri, n_boxes);
   return DM_OK;
 }
-int dm_iso_bucket(dm_iso *iso, int32_t *bstart, int32_t *btri, int32_t *bring, void *workspace,
-                  size_t workspace_bytes, void *stream) {
-  return dm::iso_bucket(iso, bstart, btri, bring, workspace, workspace_bytes, S(stream));
+int dm_iso_bucket(dm_iso *iso, int32_t *bstart, int32_t *btri, int32_t *bring, int32_t *coarse,
+                  void *workspace, size_t workspace_bytes, void *stream) {
+  return dm::iso_bucket(iso, bstart, btri, bring, coarse, workspace, workspace_bytes, S(stream));
 }
 int dm_iso_eval(const dm_iso *iso, const float *points, int32_t stride, int64_t n,
                 const int32_t *idx, const int64_t *count, float *d, float *grad, void *stream) {

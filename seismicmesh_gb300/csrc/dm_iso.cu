@@ -212,24 +212,42 @@ __global__ void k_iso_bucket_sort(int64_t nbk, const int32_t *start, int32_t *bt
   }
 }
 
-// one Jacobi pass of the Chebyshev distance transform of the non-empty boxes
-__global__ void k_iso_ring_pass(dm_iso I, const int32_t *in, int32_t *out) {
-  const int64_t nbk = (int64_t)I.nb[0] * I.nb[1] * I.nb[2];
+// one Jacobi pass of the Chebyshev distance transform of the non-empty
+// cells of a grid of nb.x x nb.y x nb.z
+__global__ void k_iso_ring_pass(int3 nb, const int32_t *in, int32_t *out) {
+  const int64_t nbk = (int64_t)nb.x * nb.y * nb.z;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbk;
        b += (int64_t)gridDim.x * blockDim.x) {
-    int z = (int)(b % I.nb[2]), y = (int)((b / I.nb[2]) % I.nb[1]),
-        x = (int)(b / ((int64_t)I.nb[2] * I.nb[1]));
+    int z = (int)(b % nb.z), y = (int)((b / nb.z) % nb.y), x = (int)(b / ((int64_t)nb.z * nb.y));
     int best = in[b];
     for (int dx = -1; dx <= 1; ++dx)
       for (int dy = -1; dy <= 1; ++dy)
         for (int dz = -1; dz <= 1; ++dz) {
           int X = x + dx, Y = y + dy, Z = z + dz;
-          if (X < 0 || Y < 0 || Z < 0 || X >= I.nb[0] || Y >= I.nb[1] || Z >= I.nb[2])
-            continue;
-          int v = in[((int64_t)X * I.nb[1] + Y) * I.nb[2] + Z];
+          if (X < 0 || Y < 0 || Z < 0 || X >= nb.x || Y >= nb.y || Z >= nb.z) continue;
+          int v = in[((int64_t)X * nb.y + Y) * nb.z + Z];
           if (v < (1 << 30)) best = min(best, v + 1);
         }
     out[b] = best;
+  }
+}
+
+// coarse block occupancy (triangles in the block's boxes) and the ring seed
+__global__ void k_iso_coarse(dm_iso I, const int32_t *bstart, int32_t *cocc, int32_t *cring) {
+  const int64_t ncb = (int64_t)I.ncb[0] * I.ncb[1] * I.ncb[2];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncb;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int cz = (int)(c % I.ncb[2]), cy = (int)((c / I.ncb[2]) % I.ncb[1]),
+              cx = (int)(c / ((int64_t)I.ncb[2] * I.ncb[1]));
+    int tot = 0;
+    for (int x = cx * I.cf; x < min(I.nb[0], (cx + 1) * I.cf); ++x)
+      for (int y = cy * I.cf; y < min(I.nb[1], (cy + 1) * I.cf); ++y) {
+        const int64_t b0 = ((int64_t)x * I.nb[1] + y) * I.nb[2];
+        const int z0 = cz * I.cf, z1 = min(I.nb[2], (cz + 1) * I.cf);
+        tot += bstart[b0 + z1] - bstart[b0 + z0];
+      }
+    cocc[c] = tot;
+    cring[c] = tot ? 0 : (1 << 30);
   }
 }
 
@@ -331,48 +349,74 @@ __device__ __forceinline__ float box_dist2(const dm_iso &I, float3 x, int bx, in
   return d2;
 }
 
-// signed distance and (optionally) its gradient at x
+__device__ __forceinline__ void scan_box(const dm_iso &I, float3 x, int64_t b, float &best2,
+                                         float3 &bestp) {
+  const int s = __ldg(I.bstart + b), e = __ldg(I.bstart + b + 1);
+  for (int q = s; q < e; ++q) {
+    const int t = __ldg(I.btri + q);
+    const float4 A = __ldg(reinterpret_cast<const float4 *>(I.tris) + 3 * t);
+    const float4 B = __ldg(reinterpret_cast<const float4 *>(I.tris) + 3 * t + 1);
+    const float4 C = __ldg(reinterpret_cast<const float4 *>(I.tris) + 3 * t + 2);
+    float3 cp = closest_on_triangle(x, make_float3(A.x, A.y, A.z), make_float3(B.x, B.y, B.z),
+                                    make_float3(C.x, C.y, C.z));
+    float3 dv = sub3(x, cp);
+    float d2 = dot3(dv, dv);
+    if (d2 < best2) {
+      best2 = d2;
+      bestp = cp;
+    }
+  }
+}
+
+// squared distance from x to block (cx, cy, cz) of cf^3 boxes (a lower bound
+// for a block cut short at the grid's end)
+__device__ __forceinline__ float block_dist2(const dm_iso &I, float3 x, int cx, int cy, int cz) {
+  float lo[3] = {I.origin[0] + cx * I.cf * I.bsize[0], I.origin[1] + cy * I.cf * I.bsize[1],
+                 I.origin[2] + cz * I.cf * I.bsize[2]};
+  float xs[3] = {x.x, x.y, x.z}, d2 = 0.f;
+  for (int d = 0; d < 3; ++d) {
+    float e = fmaxf(fmaxf(lo[d] - xs[d], xs[d] - (lo[d] + I.cf * I.bsize[d])), 0.f);
+    d2 += e * e;
+  }
+  return d2;
+}
+
+// signed distance and (optionally) its gradient at x: rings of blocks
+// around x (starting at the block ring bound), descending into the boxes of
+// blocks that hold triangles and may hold a nearer one
 __device__ float iso_distance(const dm_iso &I, float3 x, float3 *grad) {
   const int bx = bucket_of(I, x.x, 0), by = bucket_of(I, x.y, 1), bz = bucket_of(I, x.z, 2);
-  const int r0 = __ldg(I.bring + ((int64_t)bx * I.nb[1] + by) * I.nb[2] + bz);
-  const int rmax = max(max(max(bx, I.nb[0] - 1 - bx), max(by, I.nb[1] - 1 - by)),
-                       max(bz, I.nb[2] - 1 - bz));
-  const float cmin = fminf(fminf(I.bsize[0], I.bsize[1]), I.bsize[2]);
+  const int cx = bx / I.cf, cy = by / I.cf, cz = bz / I.cf;
+  const int r0 = __ldg(I.cring + ((int64_t)cx * I.ncb[1] + cy) * I.ncb[2] + cz);
+  const int rmax = max(max(max(cx, I.ncb[0] - 1 - cx), max(cy, I.ncb[1] - 1 - cy)),
+                       max(cz, I.ncb[2] - 1 - cz));
+  const float cmin = I.cf * fminf(fminf(I.bsize[0], I.bsize[1]), I.bsize[2]);
   float best2 = INFINITY;
   float3 bestp = x;
   for (int r = min(r0, rmax); r <= rmax; ++r) {
-    float lower = (float)(r - 1) * cmin - I.rho;
+    const float lower = (float)(r - 1) * cmin - I.rho;
     if (lower > 0.f && lower * lower >= best2) break;
     for (int dx = -r; dx <= r; ++dx) {
-      const int X = bx + dx;
-      if (X < 0 || X >= I.nb[0]) continue;
+      const int X = cx + dx;
+      if (X < 0 || X >= I.ncb[0]) continue;
       for (int dy = -r; dy <= r; ++dy) {
-        const int Y = by + dy;
-        if (Y < 0 || Y >= I.nb[1]) continue;
+        const int Y = cy + dy;
+        if (Y < 0 || Y >= I.ncb[1]) continue;
         const bool shell = (dx == -r || dx == r || dy == -r || dy == r);
         const int step = shell ? 1 : max(2 * r, 1);
         for (int dz = -r; dz <= r; dz += step) {
-          const int Z = bz + dz;
-          if (Z < 0 || Z >= I.nb[2]) continue;
-          float bd = sqrtf(box_dist2(I, x, X, Y, Z)) - I.rho;
+          const int Z = cz + dz;
+          if (Z < 0 || Z >= I.ncb[2]) continue;
+          if (__ldg(I.cocc + ((int64_t)X * I.ncb[1] + Y) * I.ncb[2] + Z) == 0) continue;
+          float bd = sqrtf(block_dist2(I, x, X, Y, Z)) - I.rho;
           if (bd > 0.f && bd * bd >= best2) continue;
-          const int64_t b = ((int64_t)X * I.nb[1] + Y) * I.nb[2] + Z;
-          const int s = __ldg(I.bstart + b), e = __ldg(I.bstart + b + 1);
-          for (int q = s; q < e; ++q) {
-            const int t = __ldg(I.btri + q);
-            const float4 A = __ldg(reinterpret_cast<const float4 *>(I.tris) + 3 * t);
-            const float4 B = __ldg(reinterpret_cast<const float4 *>(I.tris) + 3 * t + 1);
-            const float4 C = __ldg(reinterpret_cast<const float4 *>(I.tris) + 3 * t + 2);
-            float3 cp = closest_on_triangle(x, make_float3(A.x, A.y, A.z),
-                                            make_float3(B.x, B.y, B.z),
-                                            make_float3(C.x, C.y, C.z));
-            float3 dv = sub3(x, cp);
-            float d2 = dot3(dv, dv);
-            if (d2 < best2) {
-              best2 = d2;
-              bestp = cp;
-            }
-          }
+          for (int fx = X * I.cf; fx < min(I.nb[0], (X + 1) * I.cf); ++fx)
+            for (int fy = Y * I.cf; fy < min(I.nb[1], (Y + 1) * I.cf); ++fy)
+              for (int fz = Z * I.cf; fz < min(I.nb[2], (Z + 1) * I.cf); ++fz) {
+                float fd = sqrtf(box_dist2(I, x, fx, fy, fz)) - I.rho;
+                if (fd > 0.f && fd * fd >= best2) continue;
+                scan_box(I, x, ((int64_t)fx * I.nb[1] + fy) * I.nb[2] + fz, best2, bestp);
+              }
         }
       }
     }
@@ -463,12 +507,16 @@ size_t iso_bucket_workspace(int64_t ntri, int64_t nbk) {
   return c.used + 256;
 }
 
-int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, void *ws,
-               size_t ws_bytes, cudaStream_t s) {
-  DM_ARG_CHECK(iso_grid_ok(I) && I->tris && I->ntri >= 0 && bstart && btri && bring,
+int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, int32_t *coarse,
+               void *ws, size_t ws_bytes, cudaStream_t s) {
+  DM_ARG_CHECK(iso_grid_ok(I) && I->tris && I->ntri >= 0 && bstart && btri && bring && coarse,
                "iso buckets");
   DM_ARG_CHECK(I->nb[0] > 0 && I->nb[1] > 0 && I->nb[2] > 0 && I->bsize[0] > 0 &&
                    I->bsize[1] > 0 && I->bsize[2] > 0, "bucket grid");
+  DM_ARG_CHECK(I->cf >= 1 && I->ncb[0] == (I->nb[0] + I->cf - 1) / I->cf &&
+                   I->ncb[1] == (I->nb[1] + I->cf - 1) / I->cf &&
+                   I->ncb[2] == (I->nb[2] + I->cf - 1) / I->cf, "coarse grid");
+  const int64_t ncb = (int64_t)I->ncb[0] * I->ncb[1] * I->ncb[2];
   const int64_t nbk = (int64_t)I->nb[0] * I->nb[1] * I->nb[2];
   Carve c(ws, ws_bytes);
   int32_t *cnt = c.take<int32_t>(nbk), *key = c.take<int32_t>(I->ntri),
@@ -491,14 +539,32 @@ int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, void *
   const int passes = max(max(I->nb[0], I->nb[1]), I->nb[2]);
   int32_t *a = bring, *b = ring2;
   for (int p = 0; p < passes; ++p) {
-    k_iso_ring_pass<<<grid_for(nbk, 256), 256, 0, s>>>(*I, a, b);
+    k_iso_ring_pass<<<grid_for(nbk, 256), 256, 0, s>>>(make_int3(I->nb[0], I->nb[1], I->nb[2]),
+                                                       a, b);
     int32_t *t = a;
     a = b;
     b = t;
   }
   if (a != bring)
     DM_CUDA_TRY(cudaMemcpyAsync(bring, a, sizeof(int32_t) * nbk, cudaMemcpyDeviceToDevice, s));
-  note_launches(4 + passes);
+  // coarse level: occupancy, then its ring transform (ping-pong through ring2)
+  int32_t *cocc = coarse, *cring = coarse + ncb;
+  k_iso_coarse<<<grid_for(ncb, 128), 128, 0, s>>>(*I, bstart, cocc, cring);
+  const int cpasses = max(max(I->ncb[0], I->ncb[1]), I->ncb[2]);
+  a = cring;
+  b = ring2;
+  for (int p = 0; p < cpasses; ++p) {
+    k_iso_ring_pass<<<grid_for(ncb, 256), 256, 0, s>>>(
+        make_int3(I->ncb[0], I->ncb[1], I->ncb[2]), a, b);
+    int32_t *t = a;
+    a = b;
+    b = t;
+  }
+  if (a != cring)
+    DM_CUDA_TRY(cudaMemcpyAsync(cring, a, sizeof(int32_t) * ncb, cudaMemcpyDeviceToDevice, s));
+  I->cocc = cocc;
+  I->cring = cring;
+  note_launches(5 + passes + cpasses);
   DM_LAUNCH_CHECK();
   int rho_bits = 0;
   DM_CUDA_TRY(cudaMemcpyAsync(&rho_bits, rho, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -513,7 +579,8 @@ int iso_bucket(dm_iso *I, int32_t *bstart, int32_t *btri, int32_t *bring, void *
 
 int iso_eval(const dm_iso *I, const float *pts, int stride, int64_t n, const int32_t *idx,
              const int64_t *count_dev, float *d, float *grad, cudaStream_t s) {
-  DM_ARG_CHECK(iso_grid_ok(I) && I->tris && I->bstart && I->btri && I->bring, "iso sdf");
+  DM_ARG_CHECK(iso_grid_ok(I) && I->tris && I->bstart && I->btri && I->bring && I->cocc &&
+                   I->cring && I->cf >= 1, "iso sdf");
   DM_ARG_CHECK(pts && d && n >= 0 && stride >= 3, "points");
   if (n == 0 && !count_dev) return DM_OK;
   k_iso_eval<<<grid_for(n, 128, kSMs * 32), 128, 0, s>>>(*I, pts, stride, n, idx, count_dev,

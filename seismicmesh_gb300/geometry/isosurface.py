@@ -8,7 +8,9 @@ piecewise-linear interpolant of B over the Kuhn split of each grid cell (6
 tetrahedra along the cell's main diagonal), extracted by marching
 tetrahedra on the GPU (dm_iso_count / dm_iso_emit), and `eval` returns the
 exact signed distance to it (negative inside) by a nearest-triangle search
-over a uniform grid of boxes (dm_iso_eval).
+over a uniform grid of boxes grouped in coarse blocks: rings of blocks
+around the query, descending only into blocks that hold triangles and may
+hold a nearer one (dm_iso_eval).
 """
 import numpy as np
 import torch
@@ -24,9 +26,10 @@ class Isosurface:
     bbox = (lo0, hi0, lo1, hi1, lo2, hi2) (node (i, j, k) at lo + (i, j, k) h
     with h = (hi - lo) / (n - 1)), with exact signed distances.
 
-    box_cells: edge of the search boxes in grid cells."""
+    box_cells: edge of the search boxes in grid cells; block: edge of the
+    coarse blocks in boxes."""
 
-    def __init__(self, field, bbox, level=0.5, box_cells=4):
+    def __init__(self, field, bbox, level=0.5, box_cells=4, block=4):
         if isinstance(field, torch.Tensor):
             f = field.to(device=D.device(), dtype=torch.float32).contiguous()
         else:
@@ -64,14 +67,20 @@ class Isosurface:
             iso.nb[k] = max(1, -(-(n[k] - 1) // box_cells))
             iso.bsize[k] = box_cells * iso.h[k]
             nbk *= iso.nb[k]
+        iso.cf = block
+        ncb = 1
+        for k in range(3):
+            iso.ncb[k] = -(-iso.nb[k] // block)
+            ncb *= iso.ncb[k]
         self.bstart = D.empty((nbk + 1,), torch.int32)
         self.btri = D.empty((max(self.ntri, 1),), torch.int32)
         self.bring = D.empty((nbk,), torch.int32)
+        self.coarse = D.empty((2 * ncb,), torch.int32)
         ws = N.c_sz(0)
         N.call("dm_iso_bucket_workspace_size", self.ntri, nbk, ws)
         w = D.workspace(ws.value)
         N.call("dm_iso_bucket", iso, D.ptr(self.bstart), D.ptr(self.btri), D.ptr(self.bring),
-               D.ptr(w), w.numel(), D.stream_ptr())
+               D.ptr(self.coarse), D.ptr(w), w.numel(), D.stream_ptr())
         self.struct = iso
 
     def batched_eval(self, pts, stride, n, d, grad=None, mode=None, idx=None, count=None):

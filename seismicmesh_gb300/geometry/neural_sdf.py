@@ -32,15 +32,16 @@ class NeuralSDF:
     """MLP fit of `exact` (an object with batched_eval / bbox) for meshes with
     minimum edge length hmin."""
 
-    def __init__(self, exact, hmin, clamp=None, n_samples=4_000_000, batch=16384, epochs=12,
-                 lr=2e-3, sigma=4.0, near_fraction=0.5, near_scale=None, seed=0, margin=1.5,
-                 n_val=1 << 18, verbose=False):
+    def __init__(self, exact, hmin, clamp=None, n_samples=4_000_000, batch=16384, epochs=60,
+                 lr=5e-3, sigma=1.5, near_fraction=0.5, near_scale=None, weight_alpha=3.0,
+                 seed=0, margin=1.5, n_val=1 << 18, samples=None, val_samples=None,
+                 verbose=False):
         self.exact = exact
         self.dim = 3
         self.bbox = tuple(exact.bbox)
         self.corners = None
         self.hmin = float(hmin)
-        self.clamp = float(clamp if clamp is not None else 10.0 * hmin)
+        self.clamp = float(clamp if clamp is not None else 20.0 * hmin)
         self.margin = float(margin)
         self.verbose = verbose
         lo = np.array(self.bbox[0::2], dtype=np.float64)
@@ -67,9 +68,16 @@ class NeuralSDF:
         self.stats = {}
         self._idx = None
         self._count = D.zeros((1,), torch.int64)
-        self.train(n_samples, batch, epochs, lr, near_fraction,
-                   near_scale if near_scale is not None else 4.0 * hmin)
-        self.validate(n_val)
+        near_scale = near_scale if near_scale is not None else 8.0 * hmin
+        t0 = time.perf_counter()
+        if samples is None:
+            samples = self.make_samples(n_samples, near_fraction, near_scale)
+        torch.cuda.synchronize()
+        self.stats["samples_s"] = time.perf_counter() - t0
+        self.train(samples, batch, epochs, lr, weight_alpha)
+        if val_samples is None:
+            val_samples = self.make_samples(n_val, 0.5, near_scale)
+        self.validate(val_samples)
 
     # ------------------------------------------------------------------
     @staticmethod
@@ -85,7 +93,7 @@ class NeuralSDF:
         p[off:off + 128] = rng.normal(0.0, math.sqrt(1.0 / 128), size=128)
         return p
 
-    def _samples(self, n, near_fraction, near_scale):
+    def make_samples(self, n, near_fraction, near_scale):
         """n points (float[n][4]) : a share near the surface (a random point
         of a random triangle plus a Gaussian offset), the rest uniform in the
         box; and their exact distances"""
@@ -111,12 +119,16 @@ class NeuralSDF:
         self.exact.batched_eval(X, 4, n, d)
         return X, d
 
-    def train(self, n_samples, batch, epochs, lr, near_fraction, near_scale):
-        t0 = time.perf_counter()
-        X, d = self._samples(n_samples, near_fraction, near_scale)
-        target = torch.clamp(d, -self.clamp, self.clamp) / self.clamp
-        torch.cuda.synchronize()
+    def train(self, samples, batch, epochs, lr, weight_alpha=0.0):
+        """Adam on MSE against the clamped exact distances (in units of the
+        clamp), optionally weighted by 1 + alpha exp(-|d| / (4 hmin))"""
+        X, d = samples
+        n_samples = len(d)
         t1 = time.perf_counter()
+        target = torch.clamp(d, -self.clamp, self.clamp) / self.clamp
+        weight = None
+        if weight_alpha:
+            weight = 1.0 + weight_alpha * torch.exp(-d.abs() / (4.0 * self.hmin))
         npar = N.MLP_NPARAMS
         grads = D.zeros((npar,), torch.float32)
         m1 = D.zeros((npar,), torch.float32)
@@ -135,8 +147,9 @@ class NeuralSDF:
                 sel = perm[s * batch:(s + 1) * batch]
                 xb = X[sel]
                 tb = target[sel]
-                N.call("dm_mlp_forward_backward", self.struct, D.ptr(xb), D.ptr(tb), None, batch,
-                       D.ptr(grads), D.ptr(loss), D.ptr(w), w.numel(), D.stream_ptr())
+                wb = weight[sel] if weight is not None else None
+                N.call("dm_mlp_forward_backward", self.struct, D.ptr(xb), D.ptr(tb), D.ptr(wb),
+                       batch, D.ptr(grads), D.ptr(loss), D.ptr(w), w.numel(), D.stream_ptr())
                 step += 1
                 # cosine decay to 1 % of lr
                 lr_t = lr * (0.01 + 0.99 * 0.5 * (1 + math.cos(math.pi * step / total)))
@@ -148,13 +161,16 @@ class NeuralSDF:
         N.call("dm_mlp_to_bf16", D.ptr(self.params), D.ptr(self.wbf16), D.stream_ptr())
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        self.stats.update(samples_s=t1 - t0, train_s=t2 - t1, steps=step, epochs=epochs,
-                          batch=batch, n_samples=n_samples, loss_per_epoch=losses)
+        self.stats.update(train_s=t2 - t1, steps=step, epochs=epochs, batch=batch,
+                          n_samples=n_samples, loss_per_epoch=losses, lr=lr,
+                          weight_alpha=weight_alpha)
 
-    def validate(self, n):
-        """largest |network - clamp(exact)| on held-out samples (half near the
-        surface, half uniform), with the tensor-core inference; sets band"""
-        X, d = self._samples(n, 0.5, 4.0 * self.hmin)
+    def validate(self, samples):
+        """largest |network - clamp(exact)| on held-out samples, with the
+        tensor-core inference; sets band (infinite when the network cannot
+        separate anything from the band: every value is then exact)"""
+        X, d = samples
+        n = len(d)
         y = D.empty((n,), torch.float32)
         self.mlp_eval_device(X, 4, n, y)
         ref = torch.clamp(d, -self.clamp, self.clamp)
@@ -162,6 +178,8 @@ class NeuralSDF:
         near = d.abs() < 2 * self.hmin
         self.max_error = float(err.max().item())
         self.band = 2 * self.hmin + self.margin * self.max_error
+        if self.band >= self.clamp:
+            self.band = float("inf")
         sign_ok = ((y > 0) == (d > 0)) | (d.abs() < self.band)
         self.stats.update(
             max_abs_error=self.max_error,

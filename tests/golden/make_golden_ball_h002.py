@@ -2,11 +2,16 @@
 initial points, max_iter 50, seed 0, then sliver_removal with a 10 degree
 bound), run through oracle/ref_harness.py in the build container:
 
-    python tests/golden/make_golden_ball_h002.py      # about 40 min, 1 core
+    python tests/golden/make_golden_ball_h002.py           # about 30 min, 1 core
+    python tests/golden/make_golden_ball_h002.py --jitter  # same, generic start
 
 Writes tests/golden/ball_h002.json (counts, dihedral and quality
-statistics, volume, wall times).  The GPU test compares the package's
-generate_mesh + sliver_removal with these numbers.
+statistics, volume, wall times).  With --jitter the run starts from the
+same initial points moved by a seeded uniform jitter of +-1e-3 h (rounded
+to float32; oracle/distmesh_np.py jittered_ball_points), where every
+Delaunay triangulation of the run is unique, and writes
+ball_h002_jitter.json.  The GPU tests compare the package's generate_mesh +
+sliver_removal with these numbers.
 """
 import json
 import os
@@ -19,8 +24,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from oracle import ref_harness  # noqa: E402
+from oracle import distmesh_np as O  # noqa: E402
 from oracle import mesh_qa_np as QA  # noqa: E402
+from oracle import ref_harness  # noqa: E402
 
 SM = ref_harness.load()
 from _fast_geometry import calc_dihedral_angles  # noqa: E402
@@ -40,9 +46,11 @@ def metrics(p, t):
 
 def main():
     h = 0.02
+    jitter = "--jitter" in sys.argv
     ball = SM.Ball([0.0, 0.0, 0.0], 1.0)
+    kw = {"points": O.jittered_ball_points(h)} if jitter else {}
     t0 = time.perf_counter()
-    p, t = SM.generate_mesh(ball, h, max_iter=50, seed=0, verbose=0)
+    p, t = SM.generate_mesh(ball, h, max_iter=50, seed=0, verbose=0, **kw)
     t1 = time.perf_counter()
     m_gen = metrics(p, t)
     print("generate_mesh", t1 - t0, m_gen, flush=True)
@@ -52,14 +60,16 @@ def main():
     m_sl = metrics(p2, t2c)
     print("sliver_removal", t3 - t2, m_sl, flush=True)
     out = {
-        "workload": "3D unit ball, h=0.02, max_iter 50, seed 0, sliver_removal(min_dh_angle_bound=10)",
+        "workload": "3D unit ball, h=0.02, max_iter 50, seed 0, sliver_removal(min_dh_angle_bound=10)"
+                    + (", initial points jittered by U(-1e-3 h, 1e-3 h), seed 0" if jitter else ""),
         "engine": "reference loop (SeismicMesh generation/mesh_generator.py) with Qhull standing in for CGAL",
         "generate_mesh": m_gen, "sliver_removal": m_sl,
         "generate_mesh_s": t1 - t0, "sliver_removal_s": t3 - t2,
     }
-    with open(os.path.join(HERE, "ball_h002.json"), "w") as f:
+    name = "ball_h002_jitter.json" if jitter else "ball_h002.json"
+    with open(os.path.join(HERE, name), "w") as f:
         json.dump(out, f, indent=1)
-    print("wrote ball_h002.json")
+    print("wrote", name)
 
 
 if __name__ == "__main__":
