@@ -125,6 +125,16 @@ class ClockSampler:
         }
 
 
+def measured_peaks_all():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]),
+                "kind": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "kind": "fallback"}
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -398,6 +408,10 @@ def run_ours(args, world, rank, local):
         e2e["min_dihedral_deg"] = float(dh.min())
         e2e["mean_min_dihedral_deg"] = float(dh.mean())
 
+    salt = None
+    if not args.no_salt:
+        salt = salt_bench(measured_peaks_all())
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         ncpu, dt, _ = cpu_sample(1, 0)
@@ -451,8 +465,110 @@ def run_ours(args, world, rank, local):
             "clocks": clocks.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "neural_vs_exact": salt,
         }
         print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+SALT = {"hmin": 50.0, "wl": 10, "freq": 6.0, "grade": 0.15}
+MLP_FLOPS_PER_QUERY = 2 * 128 * (64 + 3 * 128) + 2 * 128  # the four MMA layers + output dot
+
+
+def salt_bench(peaks):
+    """The synthetic 3D salt body (676 x 676 x 210 velocity grid at 20 m;
+    its salt isosurface is the domain): time-to-mesh with the exact
+    isosurface SDF and with the neural SDF (exact inside the band and for the
+    final projection), both generate_mesh + sliver_removal at equal final
+    quality; plus the MLP tensor-core inference throughput against the bf16
+    peak and the exact SDF's query throughput."""
+    import contextlib
+
+    import torch
+
+    import seismicmesh_gb300 as sm
+    from seismicmesh_gb300 import synthetic as S
+
+    def tick():
+        torch.cuda.synchronize()
+        return time.perf_counter()
+
+    out = {"workload": "synthetic 3D salt body: velocity grid 210 x 676 x 676 (20 m nominal), "
+                       "salt = 0.5 level set of 8 seeded Gaussian bumps; sizing wl=10 at 6 Hz, "
+                       "hmin=50 m, grade 0.15; domain = the salt body"}
+    with contextlib.redirect_stdout(sys.stderr):
+        t0 = tick()
+        vp, B, bbox = S.salt_model_3d()
+        t1 = tick()
+        ef = sm.get_sizing_function_from_segy(None, bbox, velocity_data=vp, nz=vp.shape[0],
+                                              nx=vp.shape[1], ny=vp.shape[2], **SALT)
+        t2 = tick()
+        iso = sm.Isosurface(B, bbox, 0.5)
+        t3 = tick()
+        out.update(model_s=t1 - t0, sizing_s=t2 - t1, iso_build_s=t3 - t2, triangles=iso.ntri)
+        t4 = tick()
+        nn = sm.NeuralSDF(iso, SALT["hmin"])
+        t5 = tick()
+        out["mlp"] = {k: v for k, v in nn.stats.items() if k != "loss_per_epoch"}
+        out["mlp"]["build_s"] = t5 - t4
+        out["mlp"]["final_loss"] = nn.stats["loss_per_epoch"][-1]
+        for name, dom in (("exact", iso), ("neural", nn)):
+            ta = tick()
+            p, c = sm.generate_mesh(dom, ef, verbose=0)
+            tb = tick()
+            p2, c2 = sm.sliver_removal(p, dom, ef, verbose=0)
+            tc = tick()
+            st = sm.geometry.quality_stats(p2, c2)
+            out[name] = {
+                "time_to_mesh_s": tc - ta, "generate_mesh_s": tb - ta, "sliver_removal_s": tc - tb,
+                "point_iterations_per_s": len(p) * 49 / (tb - ta),
+                "n_points": int(len(p2)), "n_cells": int(len(c2)),
+                "min_dihedral_deg": st["min_dihedral"], "mean_min_dihedral_deg": st["avg_dihedral"],
+                "mean_quality": st["avg_quality"], "min_quality": st["min_quality"],
+            }
+        out["speedup_time_to_mesh"] = out["exact"]["time_to_mesh_s"] / out["neural"]["time_to_mesh_s"]
+        out["speedup_incl_training"] = out["exact"]["time_to_mesh_s"] / (
+            out["neural"]["time_to_mesh_s"] + out["mlp"]["build_s"])
+        # query throughput on 4M points uniform in the box
+        n = 1 << 22
+        g = torch.Generator(device="cuda")
+        g.manual_seed(3)
+        lo = torch.tensor(bbox[0::2], dtype=torch.float32, device="cuda")
+        hi = torch.tensor(bbox[1::2], dtype=torch.float32, device="cuda")
+        X = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        X[:, :3] = lo + (hi - lo) * torch.rand((n, 3), generator=g, device="cuda")
+        d = torch.empty(n, dtype=torch.float32, device="cuda")
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+        def timed(fn, reps):
+            fn()
+            torch.cuda.synchronize()
+            ev[0].record()
+            for _ in range(reps):
+                fn()
+            ev[1].record()
+            torch.cuda.synchronize()
+            return ev[0].elapsed_time(ev[1]) / reps
+
+        ms_mlp = timed(lambda: nn.mlp_eval_device(X, 4, n, d), 10)
+        m1 = 1 << 20
+        ms_exact = timed(lambda: iso.batched_eval(X, 4, m1, d), 1)
+        ms_neural = timed(lambda: nn.batched_eval(X, 4, m1, d), 3)
+        achieved = MLP_FLOPS_PER_QUERY * n / (ms_mlp / 1000.0) / 1e12
+        out["mlp_roofline"] = {
+            "bound": "tensor", "kernel": "k_mlp_infer_tc (tcgen05 BF16, FP32 accumulation in TMEM)",
+            "achieved": achieved, "peak": peaks["bf16_tflops"], "peak_kind": peaks["kind"],
+            "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
+            "flops_per_query": MLP_FLOPS_PER_QUERY, "queries_per_launch": n,
+            "avg_launch_ms": ms_mlp, "traffic": None,
+        }
+        out["sdf_queries_per_s"] = {
+            "uniform_points": m1, "exact": m1 / (ms_exact / 1000.0),
+            "neural_with_exact_band": m1 / (ms_neural / 1000.0),
+            "network_only": n / (ms_mlp / 1000.0),
+            "exact_fraction_in_band": int(nn._count.item()) / m1,
+        }
+    return out
 
 
 PROFILE_L1 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
@@ -531,12 +647,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-salt", action="store_true",
+                    help="skip the salt-body workload (neural vs exact SDF)")
+    ap.add_argument("--salt-only", action="store_true",
+                    help="run only the salt-body workload and print its JSON object")
     ap.add_argument("--ncu-case", action="store_true",
                     help="profiling case: the bench workload for --warmup iterations, then one "
                          "triangulation (no timing, no JSON line)")
     args = ap.parse_args()
     if args.ncu_case:
         ncu_case(args)
+        return
+    if args.salt_only:
+        print(json.dumps(salt_bench(measured_peaks_all())), flush=True)
         return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -63,6 +63,7 @@ struct DTArgs {
   const float *P;  // float4 (3D) or float2 (2D)
   GridParams *gp;
   int *bbox;          // 6 ordered ints
+  int *occ;           // occupied cells of the first grid
   int32_t *cell_of;   // [n]
   int32_t *slot;      // [n]
   int32_t *cell_cnt;  // [cap_cells]
@@ -103,6 +104,7 @@ static size_t carve_dt(Carve &c, DTArgs &a, int dim, int64_t n) {
   a.cap_blocks = a.cap_cells;
   a.gp = c.take<GridParams>(1);
   a.bbox = c.take<int>(8);
+  a.occ = c.take<int>(1);
   a.cell_of = c.take<int32_t>(n);
   a.slot = c.take<int32_t>(n);
   a.cell_cnt = c.take<int32_t>(a.cap_cells);
@@ -256,6 +258,59 @@ __global__ void k_grid_params(GridParams *gp, const int *bbox, int64_t n,
   for (int k = 0; k < 3; ++k) {
     g.lo[k] = k < dim ? (float)lo[k] : 0.f;
     g.dims[k] = k < dim ? dims[k] : 1;
+    g.ncells *= g.dims[k];
+    g.bdims[k] = (g.dims[k] + g.bs - 1) / g.bs;
+    g.nblocks *= g.bdims[k];
+  }
+  *gp = g;
+}
+
+// occupied cells of the first grid (cells holding at least one point)
+__global__ void k_occupancy(const int32_t *cnt, const GridParams *gp, int *occ) {
+  const int64_t nc = gp->ncells;
+  int c = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc;
+       i += (int64_t)gridDim.x * blockDim.x)
+    c += cnt[i] > 0;
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(occ, c);
+}
+
+// The first cell size assumes the points fill their bounding box.  When they
+// fill only part of it (a ball fills half of its cube, a salt body much
+// less), every occupied cell holds several points and the level-1 gathers
+// overflow their candidate slots.  Shrink the cells so that an occupied cell
+// holds about one point, cs *= (occupied / n)^(1/dim), within the cell
+// capacity.
+__global__ void k_grid_refine(GridParams *gp, const int *bbox, const int *occ, int64_t n,
+                              int64_t cap_cells) {
+  if (threadIdx.x != 0) return;
+  GridParams g = *gp;
+  const double ppc = (double)n / (double)max(*occ, 1);
+  if (!(ppc > 1.25)) return;
+  double ext[3] = {0, 0, 0};
+  for (int k = 0; k < g.dim; ++k) {
+    ext[k] = (double)o2f(bbox[3 + k]) - (double)o2f(bbox[k]);
+    if (!(ext[k] >= 0) || !isfinite(ext[k])) return;
+  }
+  double cs = g.cs * pow(1.0 / ppc, 1.0 / g.dim);
+  int dims[3] = {1, 1, 1};
+  for (int it = 0; it < 200; ++it) {
+    double cells = 1;
+    for (int k = 0; k < g.dim; ++k) {
+      dims[k] = (int)fmin(floor(ext[k] / cs), 1e9) + 1;
+      cells *= dims[k];
+    }
+    if (cells <= (double)cap_cells) break;
+    cs *= 1.05;
+  }
+  if (!(cs < g.cs)) return;
+  g.cs = (float)cs;
+  g.inv_cs = (float)(1.0 / cs);
+  g.ncells = 1;
+  g.nblocks = 1;
+  for (int k = 0; k < 3; ++k) {
+    g.dims[k] = k < g.dim ? dims[k] : 1;
     g.ncells *= g.dims[k];
     g.bdims[k] = (g.dims[k] + g.bs - 1) / g.bs;
     g.nblocks *= g.bdims[k];
@@ -2900,10 +2955,20 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
   else
     k_bbox<2><<<nb, 256, 0, s>>>(pts, n, a.bbox, counters);
   k_grid_params<<<1, 32, 0, s>>>(a.gp, a.bbox, n, dim, a.cap_cells, a.cap_blocks);
-  if (dim == 3)
-    k_cell_count<3><<<nb, 256, 0, s>>>(pts, n, a.gp, a.cell_of, a.slot, a.cell_cnt);
-  else
-    k_cell_count<2><<<nb, 256, 0, s>>>(pts, n, a.gp, a.cell_of, a.slot, a.cell_cnt);
+  // count once on the bounding-box grid to measure occupancy, refine the
+  // cell size, count again on the final grid
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass) {
+      DM_CUDA_TRY(cudaMemsetAsync(a.occ, 0, sizeof(int), s));
+      k_occupancy<<<grid_for(a.cap_cells, 256), 256, 0, s>>>(a.cell_cnt, a.gp, a.occ);
+      k_grid_refine<<<1, 32, 0, s>>>(a.gp, a.bbox, a.occ, n, a.cap_cells);
+      DM_CUDA_TRY(cudaMemsetAsync(a.cell_cnt, 0, sizeof(int32_t) * a.cap_cells, s));
+    }
+    if (dim == 3)
+      k_cell_count<3><<<nb, 256, 0, s>>>(pts, n, a.gp, a.cell_of, a.slot, a.cell_cnt);
+    else
+      k_cell_count<2><<<nb, 256, 0, s>>>(pts, n, a.gp, a.cell_of, a.slot, a.cell_cnt);
+  }
   DM_LAUNCH_CHECK();
   int rc = exclusive_scan_i32(a.cell_cnt, a.cell_start, a.cap_cells, a.scan_tmp, s);
   if (rc) return rc;
@@ -2933,7 +2998,7 @@ int delaunay(int dim, const float *pts, int64_t n, int32_t *cells,
     k_star2_l1<<<g1, 32 * L1_WARPS, 0, s>>>(a);
   DM_LAUNCH_CHECK();
   prof_mark(1, s);
-  int launches = 14;
+  int launches = 17;
   if (dim == 3) {
     // hull candidates bucketed by coarse block
     DM_CUDA_TRY(cudaMemsetAsync(a.o_cnt, 0, sizeof(int32_t) * a.cap_blocks, s));

@@ -381,9 +381,11 @@ __device__ __forceinline__ float block_dist2(const dm_iso &I, float3 x, int cx, 
   return d2;
 }
 
-// signed distance and (optionally) its gradient at x: rings of blocks
-// around x (starting at the block ring bound), descending into the boxes of
-// blocks that hold triangles and may hold a nearer one
+// signed distance and (optionally) its gradient at x: first the 27 boxes
+// around x (for a point near the surface they hold the nearest triangle, so
+// the bound is tight from the start), then rings of blocks around x
+// (starting at the block ring bound), descending into the boxes of blocks
+// that hold triangles and may hold a nearer one
 __device__ float iso_distance(const dm_iso &I, float3 x, float3 *grad) {
   const int bx = bucket_of(I, x.x, 0), by = bucket_of(I, x.y, 1), bz = bucket_of(I, x.z, 2);
   const int cx = bx / I.cf, cy = by / I.cf, cz = bz / I.cf;
@@ -393,6 +395,18 @@ __device__ float iso_distance(const dm_iso &I, float3 x, float3 *grad) {
   const float cmin = I.cf * fminf(fminf(I.bsize[0], I.bsize[1]), I.bsize[2]);
   float best2 = INFINITY;
   float3 bestp = x;
+  const bool near = __ldg(I.bring + ((int64_t)bx * I.nb[1] + by) * I.nb[2] + bz) <= 1;
+  if (near) {
+    for (int q = 0; q < 27; ++q) {  // the box of x first
+      const int k = (q + 13) % 27;
+      const int fx = bx + k / 9 - 1, fy = by + (k / 3) % 3 - 1, fz = bz + k % 3 - 1;
+      if (fx < 0 || fy < 0 || fz < 0 || fx >= I.nb[0] || fy >= I.nb[1] || fz >= I.nb[2])
+        continue;
+      const float fd = sqrtf(box_dist2(I, x, fx, fy, fz)) - I.rho;
+      if (fd > 0.f && fd * fd >= best2) continue;
+      scan_box(I, x, ((int64_t)fx * I.nb[1] + fy) * I.nb[2] + fz, best2, bestp);
+    }
+  }
   for (int r = min(r0, rmax); r <= rmax; ++r) {
     const float lower = (float)(r - 1) * cmin - I.rho;
     if (lower > 0.f && lower * lower >= best2) break;
@@ -413,6 +427,8 @@ __device__ float iso_distance(const dm_iso &I, float3 x, float3 *grad) {
           for (int fx = X * I.cf; fx < min(I.nb[0], (X + 1) * I.cf); ++fx)
             for (int fy = Y * I.cf; fy < min(I.nb[1], (Y + 1) * I.cf); ++fy)
               for (int fz = Z * I.cf; fz < min(I.nb[2], (Z + 1) * I.cf); ++fz) {
+                if (near && abs(fx - bx) <= 1 && abs(fy - by) <= 1 && abs(fz - bz) <= 1)
+                  continue;  // scanned above
                 float fd = sqrtf(box_dist2(I, x, fx, fy, fz)) - I.rho;
                 if (fd > 0.f && fd * fd >= best2) continue;
                 scan_box(I, x, ((int64_t)fx * I.nb[1] + fy) * I.nb[2] + fz, best2, bestp);
