@@ -411,6 +411,9 @@ def run_ours(args, world, rank, local):
     salt = None
     if not args.no_salt:
         salt = salt_bench(measured_peaks_all())
+    layered = None
+    if not args.no_layered:
+        layered = layered_bench()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -466,6 +469,7 @@ def run_ours(args, world, rank, local):
             "e2e": e2e,
             "cpu_baseline": cpu,
             "neural_vs_exact": salt,
+            "layered_2d": layered,
         }
         print(json.dumps(line), flush=True)
 
@@ -571,6 +575,50 @@ def salt_bench(peaks):
     return out
 
 
+def layered_bench():
+    """The synthetic 2D layered model (1911 x 5395 cells): sizing build and
+    generate_mesh on its Rectangle, time-to-mesh and point-iterations/s.  The
+    reference loop's own time on this input, measured in the build container
+    (reference loop + Qhull, one x86 core), is carried from
+    tests/golden/layered2d.json for context; it is not timed here."""
+    import contextlib
+
+    import torch
+
+    import seismicmesh_gb300 as sm
+    from seismicmesh_gb300 import synthetic
+
+    def tick():
+        torch.cuda.synchronize()
+        return time.perf_counter()
+
+    vp, bbox = synthetic.layered_model_2d(0)
+    with contextlib.redirect_stdout(sys.stderr):
+        t0 = tick()
+        ef = sm.get_sizing_function_from_segy(None, bbox, velocity_data=vp, nz=vp.shape[0],
+                                              nx=vp.shape[1], hmin=75.0, wl=10, freq=2.0,
+                                              grade=0.15)
+        t1 = tick()
+        p, t = sm.generate_mesh(sm.Rectangle(bbox), ef, verbose=0)
+        t2 = tick()
+    q = sm.geometry.simp_qual(p, t)
+    out = {"workload": "2D layered model 1911 x 5395 (synthetic, seed 0), wl=10 at 2 Hz, "
+                       "hmin=75 m, grade 0.15, Rectangle(bbox), max_iter 50",
+           "sizing_s": t1 - t0, "generate_mesh_s": t2 - t1, "time_to_mesh_s": t2 - t0,
+           "point_iterations_per_s": len(p) * 49 / (t2 - t1),
+           "n_points": int(len(p)), "n_cells": int(len(t)),
+           "min_quality": float(q.min()), "mean_quality": float(q.mean())}
+    gpath = os.path.join(ROOT, "tests", "golden", "layered2d.json")
+    if os.path.exists(gpath):
+        with open(gpath) as f:
+            g = json.load(f)
+        out["reference_build_container"] = {
+            "time_to_mesh_s": g["sizing_s"] + g["generate_mesh_s"], "n_points": g["n_points"],
+            "mean_quality": g["mean_quality"],
+            "how": "reference loop + Qhull, 1 x86 core, measured when the golden was made"}
+    return out
+
+
 PROFILE_L1 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
                           "k_star3_l1_ball_h002.md")
 PROFILE_L2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
@@ -615,13 +663,40 @@ def measured_traffic():
 
 
 def ncu_case(args):
-    """the bench workload (3D unit ball, h = 0.02) for args.warmup iterations,
-    then one more triangulation: the launch an ncu capture selects"""
+    """Profiling cases (no timing, no JSON line).
+
+    ball: the bench workload (3D unit ball, h = 0.02) for args.warmup
+          iterations, then one more full iteration (triangulation, filter,
+          adjacency, bar sums, update): the launches an ncu capture selects.
+    mlp:  the salt body's network trained briefly, then dm_mlp_eval on 2^22
+          points uniform in the box, args.warmup + 1 times."""
     import torch
 
     import seismicmesh_gb300 as sm
     from seismicmesh_gb300.generation import mesh_generator as MG
 
+    if args.ncu_case == "mlp":
+        import contextlib
+
+        from seismicmesh_gb300 import synthetic as S
+
+        with contextlib.redirect_stdout(sys.stderr):
+            vp, B, bbox = S.salt_model_3d()
+            iso = sm.Isosurface(B, bbox, 0.5)
+            nn = sm.NeuralSDF(iso, SALT["hmin"], n_samples=1 << 20, epochs=2, n_val=1 << 14)
+        n = 1 << 22
+        g = torch.Generator(device="cuda")
+        g.manual_seed(3)
+        lo = torch.tensor(bbox[0::2], dtype=torch.float32, device="cuda")
+        hi = torch.tensor(bbox[1::2], dtype=torch.float32, device="cuda")
+        X = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        X[:, :3] = lo + (hi - lo) * torch.rand((n, 3), generator=g, device="cuda")
+        d = torch.empty(n, dtype=torch.float32, device="cuda")
+        for _ in range(args.warmup + 1):
+            nn.mlp_eval_device(X, 4, n, d)
+        torch.cuda.synchronize()
+        print("ncu case done:", n, "points", flush=True)
+        return
     ball = sm.Ball([0.0, 0.0, 0.0], 1.0)
     fd = MG._Domain(ball)
     sizing = MG._Sizing(H, 3)
@@ -629,12 +704,11 @@ def ncu_case(args):
     p0 = MG._initialize_points(3, 0.1 * H, np.array([[-1.0, 1.0]] * 3), sizing, fd, H, opts, np.empty((0, 3)))
     eng = MG._Engine(3, p0, 0)
     deps = float(np.sqrt(np.finfo(float).eps) * H)
-    for _ in range(args.warmup):
+    for _ in range(args.warmup + 1):
         eng.triangulate()
         eng.filter(fd, 0.1 * H)
         eng.build_adjacency()
         eng.step(sizing, [fd], 1 + 0.4 / 2**2, 0.30, H, deps)
-    eng.triangulate()
     torch.cuda.synchronize()
     print("ncu case done:", eng.n, "points", int(eng.counters_host()[0]), "cells")
 
@@ -649,11 +723,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-salt", action="store_true",
                     help="skip the salt-body workload (neural vs exact SDF)")
+    ap.add_argument("--no-layered", action="store_true",
+                    help="skip the 2D layered-model workload")
     ap.add_argument("--salt-only", action="store_true",
                     help="run only the salt-body workload and print its JSON object")
-    ap.add_argument("--ncu-case", action="store_true",
-                    help="profiling case: the bench workload for --warmup iterations, then one "
-                         "triangulation (no timing, no JSON line)")
+    ap.add_argument("--ncu-case", choices=["ball", "mlp"], default=None,
+                    help="profiling case: ball (the bench workload for --warmup iterations, then "
+                         "one more) or mlp (tensor-core inference on 2^22 points); no timing, "
+                         "no JSON line")
     args = ap.parse_args()
     if args.ncu_case:
         ncu_case(args)

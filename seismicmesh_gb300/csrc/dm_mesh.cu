@@ -165,16 +165,69 @@ __device__ __forceinline__ void warp_bitonic(int *b, int size, int lane) {
     }
 }
 
+// One thread per vertex: its raw segment goes into a sorted, duplicate-free
+// array by insertion.  A vertex whose segment exceeds kAdjRaw entries or
+// whose unique neighbours exceed kAdjLocal is appended to big[] for the warp
+// kernel below.  The row keeps the adj_cap smallest neighbours either way.
+constexpr int kAdjLocal = 32, kAdjRaw = 160;
+__global__ void __launch_bounds__(256)
+    k_adj_dedup_thread(int64_t n, const int32_t *off, const int32_t *raw, int32_t *adj,
+                       int adj_cap, int32_t *deg, int32_t *big, int32_t *nbig,
+                       int64_t *counters) {
+  unsigned long long ecount = 0;
+  bool ovf = false;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int o = off[v], L = off[v + 1] - o;
+    int u[kAdjLocal];
+    int m = 0;
+    bool spill = L > kAdjRaw;
+    for (int k = 0; k < L && !spill; ++k) {
+      const int x = raw[o + k];
+      int j = m;
+      while (j > 0 && u[j - 1] > x) --j;
+      if (j > 0 && u[j - 1] == x) continue;
+      if (m == kAdjLocal) {
+        spill = true;
+        break;
+      }
+      for (int t = m; t > j; --t) u[t] = u[t - 1];
+      u[j] = x;
+      ++m;
+    }
+    if (spill) {
+      big[atomicAdd(nbig, 1)] = (int32_t)v;
+      continue;
+    }
+    int32_t *row = adj + v * adj_cap;
+    const int keep = min(m, adj_cap);
+    for (int i = 0; i < keep; ++i) row[i] = u[i];
+    deg[v] = keep;
+    if (m > adj_cap) ovf = true;
+    ecount += m;
+  }
+  for (int o = 16; o; o >>= 1) ecount += __shfl_xor_sync(0xffffffffu, ecount, o);
+  if ((threadIdx.x & 31) == 0 && ecount)
+    atomicAdd((unsigned long long *)&counters[DM_CNT_EDGES], ecount);
+  if (__any_sync(0xffffffffu, ovf) && (threadIdx.x & 31) == 0)
+    flag_or(counters, DM_FLAG_ADJ_OVERFLOW);
+}
+
+// One warp per listed vertex (the high-incidence ones): bitonic sort of the
+// segment in shared memory, then unique and compaction into the row.
 __global__ void __launch_bounds__(32 * ADJ_WARPS)
-    k_adj_dedup(int64_t n, const int32_t *off, const int32_t *raw, int32_t *adj,
-                int adj_cap, int32_t *deg, int64_t *counters) {
+    k_adj_dedup(const int32_t *list, const int32_t *nlist, const int32_t *off,
+                const int32_t *raw, int32_t *adj, int adj_cap, int32_t *deg,
+                int64_t *counters) {
   __shared__ int buf[ADJ_WARPS][ADJ_SORTMAX];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int *b = buf[w];
   unsigned long long ecount = 0;
   bool ovf = false;
-  for (int64_t v = (int64_t)blockIdx.x * ADJ_WARPS + w; v < n;
-       v += (int64_t)gridDim.x * ADJ_WARPS) {
+  const int64_t nl = *nlist;
+  for (int64_t q = (int64_t)blockIdx.x * ADJ_WARPS + w; q < nl;
+       q += (int64_t)gridDim.x * ADJ_WARPS) {
+    const int64_t v = list[q];
     const int o = off[v], L = off[v + 1] - o;
     int m;  // entries staged in b
     if (L <= ADJ_SORTMAX) {
@@ -707,20 +760,23 @@ int cell_centroids(int dim, const float *P, const int32_t *cells, int64_t cap,
   return DM_OK;
 }
 
+// cnt: counts, then fill cursors, then the list of high-incidence vertices;
+// tmp: scan scratch followed by the list length
 static size_t carve_adj(Carve &c, int dim, int64_t n, int64_t cap_cells, int32_t **cnt,
-                        int32_t **off, int32_t **raw, int32_t **tmp) {
+                        int32_t **off, int32_t **raw, int32_t **tmp, int32_t **nbig) {
   const int NV = dim + 1;
   *cnt = c.take<int32_t>(n);
   *off = c.take<int32_t>(n + 1);
   *raw = c.take<int32_t>((size_t)NV * (NV - 1) * cap_cells);
   *tmp = c.take<int32_t>(scan_tmp_elems(n));
+  *nbig = c.take<int32_t>(1);
   return c.used;
 }
 
 size_t adjacency_workspace(int dim, int64_t n, int64_t cap_cells) {
   Carve c(nullptr, 0);
-  int32_t *a, *b, *d, *e;
-  return carve_adj(c, dim, n, cap_cells, &a, &b, &d, &e) + 256;
+  int32_t *a, *b, *d, *e, *f;
+  return carve_adj(c, dim, n, cap_cells, &a, &b, &d, &e, &f) + 256;
 }
 
 int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
@@ -732,8 +788,8 @@ int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
   DM_ARG_CHECK(n >= 0 && n < (1 << 30) && cap_cells >= 0, "sizes");
   DM_ARG_CHECK((dim + 1) * dim * cap_cells < (1ll << 31), "too many cells");
   Carve c(ws, ws_bytes);
-  int32_t *cnt, *off, *raw, *tmp;
-  carve_adj(c, dim, n, cap_cells, &cnt, &off, &raw, &tmp);
+  int32_t *cnt, *off, *raw, *tmp, *nbig;
+  carve_adj(c, dim, n, cap_cells, &cnt, &off, &raw, &tmp, &nbig);
   if (!c.ok() || !ws) {
     set_error("adjacency: workspace %zu < required %zu", ws_bytes, c.used);
     return DM_ERR_WORKSPACE;
@@ -753,11 +809,14 @@ int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
     k_adj_fill<4><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index, off, cnt, raw);
   else
     k_adj_fill<3><<<nb, 256, 0, s>>>(cells, cap_cells, counters, count_index, off, cnt, raw);
-  int nw = grid_for(n, ADJ_WARPS);
-  k_adj_dedup<<<nw, 32 * ADJ_WARPS, 0, s>>>(n, off, raw, adj, adj_cap, deg, counters);
+  DM_CUDA_TRY(cudaMemsetAsync(nbig, 0, sizeof(int32_t), s));
+  k_adj_dedup_thread<<<grid_for(n, 256), 256, 0, s>>>(n, off, raw, adj, adj_cap, deg, cnt, nbig,
+                                                      counters);
+  k_adj_dedup<<<kSMs * 4, 32 * ADJ_WARPS, 0, s>>>(cnt, nbig, off, raw, adj, adj_cap, deg,
+                                                   counters);
   k_half_edges<<<1, 1, 0, s>>>(counters);
   DM_LAUNCH_CHECK();
-  note_launches(7);
+  note_launches(8);
   return DM_OK;
 }
 

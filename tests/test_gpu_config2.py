@@ -1,0 +1,41 @@
+"""Config 2 at full size: the synthetic 2D layered model (1911 x 5395 cells,
+8 layers 1500 -> 4500 m/s with N(0, 50) noise and an ellipse of salt),
+wavelength sizing at 10 points per wavelength at 2 Hz, hmin 75 m, grade
+0.15, meshed on its Rectangle by generate_mesh (max_iter 50, seed 0).
+
+Against the reference's own run (tests/golden/layered2d.json, made by
+tests/golden/make_golden_layered2d.py): vertex and cell counts and mean
+quality within 1 %, minimum quality within 5 % (one cell; the reference's
+termination deletes boundary cells below 0.15 and smooths), area within
+1e-6."""
+import contextlib
+import io
+import json
+import os
+
+import numpy as np
+import pytest
+
+import seismicmesh_gb300 as sm
+from conftest import GOLDEN
+from seismicmesh_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def test_layered_model_2d_matches_reference(cuda):
+    with open(os.path.join(GOLDEN, "layered2d.json")) as f:
+        g = json.load(f)
+    vp, bbox = synthetic.layered_model_2d(0)
+    with contextlib.redirect_stdout(io.StringIO()):
+        ef = sm.get_sizing_function_from_segy(None, bbox, velocity_data=vp, nz=vp.shape[0],
+                                              nx=vp.shape[1], hmin=75.0, wl=10, freq=2.0,
+                                              grade=0.15)
+    p, t = sm.generate_mesh(sm.Rectangle(bbox), ef, verbose=0)
+    q = sm.geometry.simp_qual(p, t)
+    got = {"n_points": len(p), "n_cells": len(t), "mean_quality": float(q.mean()),
+           "min_quality": float(q.min()), "area": float(np.abs(sm.geometry.simp_vol(p, t)).sum())}
+    for k, rel in (("n_points", 0.01), ("n_cells", 0.01), ("mean_quality", 0.01),
+                   ("min_quality", 0.05), ("area", 1e-6)):
+        print(f"{k}: gpu {got[k]} reference {g[k]} rel {(got[k] - g[k]) / g[k]:+.3e}")
+        assert abs(got[k] - g[k]) <= rel * abs(g[k]), (k, got[k], g[k])
