@@ -619,6 +619,40 @@ def layered_bench():
     return out
 
 
+def batch_bench(half):
+    """The batched workload: 256 independent CSG domains (the first 128 2D,
+    the rest 3D; vertex counts log-uniform over 2e3-2e5) meshed together by
+    generate_meshes; half selects the 2D or 3D half.  point-iterations/s
+    over the graph-captured iterations: the batch's points times the graph
+    iterations over their wall time."""
+    import torch
+
+    from seismicmesh_gb300 import synthetic
+    from seismicmesh_gb300.generation.batch import generate_meshes
+
+    probs = synthetic.batch_domains(256)
+    probs = probs[:128] if half == "2d" else probs[128:] if half == "3d" else probs
+    st = {}
+    t0 = time.perf_counter()
+    out = generate_meshes(probs, stats=st)
+    torch.cuda.synchronize()
+    total = time.perf_counter() - t0
+    pts = np.array(st["points"])
+    n_graph = len(st["graph_ms"])
+    return {
+        "workload": f"batched CSG domains ({half}): {len(probs)} problems, seeds 0..255",
+        "problems": len(probs), "meshed": sum(o is not None for o in out),
+        "failed": st["failed"], "points": int(pts.sum()), "min_points": int(pts.min()),
+        "max_points": int(pts.max()), "total_s": total, "setup_s": st["setup_s"],
+        "checked_iterations_s": st["checked_s"], "graph_iterations_s": st["graph_iterations_s"],
+        "termination_s": st["termination_s"], "graph_iterations": n_graph,
+        "graph_ms_median": float(np.median(st["graph_ms"])) if n_graph else None,
+        "point_iterations_per_s": float(pts.sum() * n_graph / st["graph_iterations_s"])
+        if n_graph else None,
+        "tuning": st["tuning"], "streams": st["streams"], "redone": st["redone"],
+    }
+
+
 PROFILE_L1 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
                           "k_star3_l1_ball_h002.md")
 PROFILE_L2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
@@ -725,6 +759,9 @@ def main():
                     help="skip the salt-body workload (neural vs exact SDF)")
     ap.add_argument("--no-layered", action="store_true",
                     help="skip the 2D layered-model workload")
+    ap.add_argument("--batch-only", choices=["2d", "3d", "all"], default=None,
+                    help="run only the batched workload (256 CSG domains, or its 2D or 3D half) "
+                         "and print its JSON object")
     ap.add_argument("--salt-only", action="store_true",
                     help="run only the salt-body workload and print its JSON object")
     ap.add_argument("--ncu-case", choices=["ball", "mlp"], default=None,
@@ -737,6 +774,9 @@ def main():
         return
     if args.salt_only:
         print(json.dumps(salt_bench(measured_peaks_all())), flush=True)
+        return
+    if args.batch_only:
+        print(json.dumps(batch_bench(args.batch_only)), flush=True)
         return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

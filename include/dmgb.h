@@ -42,6 +42,7 @@ extern "C" {
 #define DM_CNT_BAD 5         /* cells flagged by dm_dihedral_flags         */
 #define DM_CNT_DUPS 6        /* duplicate points found by dm_delaunay      */
 #define DM_CNT_AUX 7
+#define DM_CNT_MAXDEG 13     /* largest neighbour count seen by dm_adjacency */
 #define DM_NCOUNTERS 16
 
 /* grid_exp value that disables position rounding (dm_update_points,

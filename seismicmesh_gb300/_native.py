@@ -29,6 +29,7 @@ DM_ERR_WORKSPACE = 6
 DM_NO_GRID = -1000
 
 CNT_CELLS, CNT_ESCALATED, CNT_FLAGS, CNT_KEPT, CNT_EDGES, CNT_BAD, CNT_DUPS, CNT_AUX = range(8)
+CNT_MAXDEG = 13
 NCOUNTERS = 16
 
 FLAG_CELL_OVERFLOW = 1

@@ -53,7 +53,7 @@ struct GridParams {
 constexpr int kNoFix = -100000;
 
 // level-3 star storage: per-warp slots in the workspace
-constexpr int L3_CAP_TRI = 4096, L3_CAP_OPEN = 2048, L3_WARPS = 4, L3_BLOCKS = 76;
+constexpr int L3_CAP_TRI = 16384, L3_CAP_OPEN = 8192, L3_WARPS = 4, L3_BLOCKS = 38;
 constexpr int kCntL3 = 11;  // counters slot: stars deferred to level 3
 constexpr int kCntL2Next = 12;  // counters slot: next escalated star for level 2 (3D)
 
@@ -2345,83 +2345,101 @@ __device__ __forceinline__ void ring_search(const DTArgs &A, const GridParams &g
   }
 }
 
-// global seed from the nearest neighbour q1 and the smallest circumcircle
+// global seed from a nearest neighbour q1 and a smallest circumcircle
 // through (p, q1): for points in general position the triangle (p, q1, q2)
 // is Delaunay and both cells on its sides are found by exhaustive queries;
-// the candidate cell is verified empty over the whole point set.
+// the candidate cell is verified empty over the whole point set.  On
+// degenerate sets (a lattice: many neighbours at the same distance, many
+// circles of the same radius) the first pick may be a triangle the
+// perturbed triangulation does not contain, so the next candidates are
+// tried: up to kSeedQ2 choices of q2 for each of up to kSeedQ1 choices of
+// q1, each excluding the ones already tried.
+constexpr int kSeedQ1 = 4, kSeedQ2 = 8;
 __device__ __forceinline__ bool gseed3_nn(const DTArgs &A, const GridParams &g, int ip,
                                           int lane, int &ovf, dmp::ExactScratch *W,
                                           int3 &out) {
   float px[3];
   load_pt<3>(A.P, ip, px);
-  float bk = FLT_MAX;
-  int bj = -1, bg = 0x7fffffff;
-  ring_search<3>(A, g, px, lane,
-                 [&](int j) {
-                   if (j == ip || A.dup[j]) return;
-                   float y[3];
-                   load_pt<3>(A.P, j, y);
-                   float d = (y[0] - px[0]) * (y[0] - px[0]) + (y[1] - px[1]) * (y[1] - px[1]) +
-                             (y[2] - px[2]) * (y[2] - px[2]);
-                   if (bj < 0 || d < bk || (d == bk && j < bg)) {
-                     bk = d;
-                     bj = j;
-                     bg = j;
-                   }
-                 },
-                 [&](float guard) {
-                   float k2 = bk;
-                   int j2 = bj, g2 = bg;
-                   warp_argmin(k2, j2, g2);
-                   return j2 >= 0 && sqrtf(k2) < guard;
-                 });
-  warp_argmin(bk, bj, bg);
-  if (bj < 0) return false;
-  const int q1 = bj;
-  float a[3];
-  load_pt<3>(A.P, q1, a);
-  float A3[3] = {a[0] - px[0], a[1] - px[1], a[2] - px[2]};
-  float m[3] = {0.5f * (a[0] + px[0]), 0.5f * (a[1] + px[1]), 0.5f * (a[2] + px[2])};
-  float ck = FLT_MAX;
-  int cj = -1, cg = 0x7fffffff;
-  ring_search<3>(A, g, m, lane,
-                 [&](int j) {
-                   if (j == ip || j == q1 || A.dup[j]) return;
-                   float y[3];
-                   load_pt<3>(A.P, j, y);
-                   float B[3] = {y[0] - px[0], y[1] - px[1], y[2] - px[2]};
-                   float cx = A3[1] * B[2] - A3[2] * B[1], cy = A3[2] * B[0] - A3[0] * B[2],
-                         cz = A3[0] * B[1] - A3[1] * B[0];
-                   float cr = cx * cx + cy * cy + cz * cz;
-                   if (!(cr > 0.f)) return;
-                   float la = A3[0] * A3[0] + A3[1] * A3[1] + A3[2] * A3[2];
-                   float lb = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
-                   float dx = A3[0] - B[0], dy = A3[1] - B[1], dz = A3[2] - B[2];
-                   float R2 = la * lb * (dx * dx + dy * dy + dz * dz) / (4.f * cr);
-                   if (cj < 0 || R2 < ck || (R2 == ck && j < cg)) {
-                     ck = R2;
-                     cj = j;
-                     cg = j;
-                   }
-                 },
-                 [&](float guard) {
-                   float k2 = ck;
-                   int j2 = cj, g2 = cg;
-                   warp_argmin(k2, j2, g2);
-                   // a smaller circumcircle through p and q1 lies within 2R of m
-                   return j2 >= 0 && 2.f * sqrtf(k2) * 1.0001f < guard;
-                 });
-  warp_argmin(ck, cj, cg);
-  if (cj < 0) return false;
-  const int q2 = cj;
-  for (int side = 0; side < 2; ++side) {
-    int u = side ? q2 : q1, v = side ? q1 : q2;
-    int x = gq3(A, g, ip, u, v, lane, ovf, W);
-    if (x < 0) continue;
-    int vv[3] = {u, v, x};
-    if (gempty<3>(A, g, ip, vv, lane, ovf, W)) {
-      out = make_int3(u, v, x);
-      return true;
+  int ex1[kSeedQ1];
+  for (int a1 = 0; a1 < kSeedQ1; ++a1) {
+    float bk = FLT_MAX;
+    int bj = -1, bg = 0x7fffffff;
+    ring_search<3>(A, g, px, lane,
+                   [&](int j) {
+                     if (j == ip || A.dup[j]) return;
+                     for (int e = 0; e < a1; ++e)
+                       if (ex1[e] == j) return;
+                     float y[3];
+                     load_pt<3>(A.P, j, y);
+                     float d = (y[0] - px[0]) * (y[0] - px[0]) + (y[1] - px[1]) * (y[1] - px[1]) +
+                               (y[2] - px[2]) * (y[2] - px[2]);
+                     if (bj < 0 || d < bk || (d == bk && j < bg)) {
+                       bk = d;
+                       bj = j;
+                       bg = j;
+                     }
+                   },
+                   [&](float guard) {
+                     float k2 = bk;
+                     int j2 = bj, g2 = bg;
+                     warp_argmin(k2, j2, g2);
+                     return j2 >= 0 && sqrtf(k2) < guard;
+                   });
+    warp_argmin(bk, bj, bg);
+    if (bj < 0) return false;
+    const int q1 = bj;
+    ex1[a1] = q1;
+    float a[3];
+    load_pt<3>(A.P, q1, a);
+    const float A3[3] = {a[0] - px[0], a[1] - px[1], a[2] - px[2]};
+    const float m[3] = {0.5f * (a[0] + px[0]), 0.5f * (a[1] + px[1]), 0.5f * (a[2] + px[2])};
+    int ex2[kSeedQ2];
+    for (int a2 = 0; a2 < kSeedQ2; ++a2) {
+      float ck = FLT_MAX;
+      int cj = -1, cg = 0x7fffffff;
+      ring_search<3>(A, g, m, lane,
+                     [&](int j) {
+                       if (j == ip || j == q1 || A.dup[j]) return;
+                       for (int e = 0; e < a2; ++e)
+                         if (ex2[e] == j) return;
+                       float y[3];
+                       load_pt<3>(A.P, j, y);
+                       float B[3] = {y[0] - px[0], y[1] - px[1], y[2] - px[2]};
+                       float cx = A3[1] * B[2] - A3[2] * B[1], cy = A3[2] * B[0] - A3[0] * B[2],
+                             cz = A3[0] * B[1] - A3[1] * B[0];
+                       float cr = cx * cx + cy * cy + cz * cz;
+                       if (!(cr > 0.f)) return;
+                       float la = A3[0] * A3[0] + A3[1] * A3[1] + A3[2] * A3[2];
+                       float lb = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+                       float dx = A3[0] - B[0], dy = A3[1] - B[1], dz = A3[2] - B[2];
+                       float R2 = la * lb * (dx * dx + dy * dy + dz * dz) / (4.f * cr);
+                       if (cj < 0 || R2 < ck || (R2 == ck && j < cg)) {
+                         ck = R2;
+                         cj = j;
+                         cg = j;
+                       }
+                     },
+                     [&](float guard) {
+                       float k2 = ck;
+                       int j2 = cj, g2 = cg;
+                       warp_argmin(k2, j2, g2);
+                       // a smaller circumcircle through p and q1 lies within 2R of m
+                       return j2 >= 0 && 2.f * sqrtf(k2) * 1.0001f < guard;
+                     });
+      warp_argmin(ck, cj, cg);
+      if (cj < 0) break;
+      const int q2 = cj;
+      ex2[a2] = q2;
+      for (int side = 0; side < 2; ++side) {
+        int u = side ? q2 : q1, v = side ? q1 : q2;
+        int x = gq3(A, g, ip, u, v, lane, ovf, W);
+        if (x < 0) continue;
+        int vv[3] = {u, v, x};
+        if (gempty<3>(A, g, ip, vv, lane, ovf, W)) {
+          out = make_int3(u, v, x);
+          return true;
+        }
+      }
     }
   }
   return false;

@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(256)
       big[atomicAdd(nbig, 1)] = (int32_t)v;
       continue;
     }
+    if (m > adj_cap) atomicMax((unsigned long long *)&counters[DM_CNT_MAXDEG], (unsigned long long)m);
     int32_t *row = adj + v * adj_cap;
     const int keep = min(m, adj_cap);
     for (int i = 0; i < keep; ++i) row[i] = u[i];
@@ -268,6 +269,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS)
       base += __popc(mk);
     }
     if (base > adj_cap) ovf = true;
+    if (lane == 0 && base > adj_cap)
+      atomicMax((unsigned long long *)&counters[DM_CNT_MAXDEG], (unsigned long long)base);
     if (lane == 0) deg[v] = min(base, adj_cap);
     ecount += base;
     __syncwarp();
@@ -795,6 +798,7 @@ int adjacency(int dim, int64_t n, const int32_t *cells, int64_t cap_cells,
     return DM_ERR_WORKSPACE;
   }
   DM_CUDA_TRY(cudaMemsetAsync(&counters[DM_CNT_EDGES], 0, sizeof(int64_t), s));
+  DM_CUDA_TRY(cudaMemsetAsync(&counters[DM_CNT_MAXDEG], 0, sizeof(int64_t), s));
   if (n == 0) return DM_OK;
   DM_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
   int nb = grid_for(cap_cells, 256);

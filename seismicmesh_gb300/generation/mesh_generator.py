@@ -164,6 +164,9 @@ def _project_points_back_host(p, fd, deps, hmin, idx):
     return p
 
 
+MAX_ADJ_CAP = 4096
+
+
 class _Engine:
     """Device state of one meshing run.  With grid=True the points live on the
     position grid of the run (snapped here, kept there by the update
@@ -293,11 +296,23 @@ class _Engine:
         than the row stride."""
         while True:
             self.adjacency_async()
-            flags = int(self.counters[N.CNT_FLAGS].item())
+            c = self.counters_host()
+            flags = int(c[N.CNT_FLAGS])
             if not flags & N.FLAG_ADJ_OVERFLOW:
                 return
             self.counters[N.CNT_FLAGS] = flags & ~N.FLAG_ADJ_OVERFLOW
-            self.adj_cap *= 2
+            need = max(int(c[N.CNT_MAXDEG]), self.adj_cap + 1)
+            cap = 1 << (need - 1).bit_length()
+            rows = 4 * self.n * cap
+            free, _ = torch.cuda.mem_get_info()
+            if cap > MAX_ADJ_CAP or rows > free // 2:
+                # a vertex adjacent to thousands of others: no DistMesh
+                # iteration of a sound triangulation has one
+                raise N.NativeError(
+                    "dm_adjacency", N.DM_ERR_CAPACITY,
+                    f"a vertex has {need} neighbours (rows are limited to {MAX_ADJ_CAP}; "
+                    f"{cap} for {self.n} vertices would need {rows / 2**30:.1f} GiB)")
+            self.adj_cap = cap
 
     def slot_sizes(self, sizing):
         """per adjacency slot h(midpoint) for host-callable sizing functions"""
@@ -521,87 +536,142 @@ def generate_mesh(domain, edge_length, comm=None, **kwargs):  # noqa: C901
     def print_msg2(msg):
         print(msg, flush=True)
 
-    fd, bbox0, corners = _unpack_domain(domain, gen_opts)
-    fh, bbox1, hmin, lsf = _unpack_sizing(edge_length)
-
-    bbox = bbox0 if bbox1 is None else _minmax(bbox0, bbox1)
-    if not isinstance(bbox, tuple):
-        raise ValueError("`bbox` must be a tuple")
-    dim = int(len(bbox) / 2)
-
-    if not np.isscalar(edge_length) and dim == 3:
-        corners = None
-
-    if bbox0 != bbox1 and bbox1 is not None:
-        fd = _Domain(geometry.Rectangle(bbox) if dim == 2 else geometry.Cube(bbox))
-
-    bbox = np.array(bbox).reshape(-1, 2)
-    h0 = hmin if hmin is not None else gen_opts["h0"]
-    if h0 < 0:
-        raise ValueError("`h0` must be > 0")
-
-    L0mult = 1 + 0.4 / 2 ** (dim - 1)
-    delta_t = gen_opts["delta_t"]
-    geps = gen_opts["geps_mult"] * h0
-    deps = np.sqrt(np.finfo(np.double).eps) * h0
-
-    sizing = _Sizing(edge_length, dim)
-
-    pfix, nfix = _unpack_pfix(dim, gen_opts)
-    if corners is not None:
-        corners = corners[fd(corners) > -1000 * deps]
-        pfix = np.append(pfix, corners, axis=0)
-        nfix = len(pfix)
-    print_msg1(f"Constraining {nfix} fixed points...")
-
-    p = _initialize_points(dim, geps, bbox, sizing, fd, h0, gen_opts, pfix)
-
-    if gen_opts["max_iter"] < 0:
-        raise ValueError("`max_iter` must be > 0")
-    max_iter = gen_opts["max_iter"]
-    N_pts = p.shape[0]
-    assert N_pts > 0, "No vertices to mesh with!"
-    print_msg1("Commencing mesh generation with %d vertices on rank %d." % (N_pts, 0))
-
-    levels = [fd]
-    if gen_opts["subdomains"] is not None:
-        for sub in gen_opts["subdomains"]:
-            sfd, _, _ = _unpack_domain(sub, gen_opts)
-            levels.append(sfd)
-    batched = fd.is_batched
-    if batched and len(levels) > 1:
-        raise NotImplementedError("subdomains are not supported with a batched-SDF domain")
-    # a host-callable level moves the projection to the host (slow path)
-    host_levels = not batched and not all(lv.is_program for lv in levels)
-    if host_levels:
-        print_msg1("Host-callable domain: the Newton projection runs on the host")
-
-    eng = _Engine(dim, p, nfix)
+    run = _Run(domain, edge_length, gen_opts, print_msg1)
     count = 0
-    while True:
+    while count < run.max_iter - 1:
         start = time.time()
+        run.iterate(count, print_msg2)
+        count += 1
+        print_msg2("     Elapsed wall-clock time %f : " % (time.time() - start))
+    run.finish(print_msg1)
+    return run.eng.result()
+
+
+class _Run:
+    """One generate_mesh problem (generation/mesh_generator.py:291-529): the
+    set-up, one DistMesh iteration (checked: duplicates, capacities and row
+    widths handled on the host), the same iteration as a host-synchronisation
+    free launch sequence for CUDA-graph capture, and the termination."""
+
+    def __init__(self, domain, edge_length, gen_opts, print_msg1=lambda m: None):
+        self.opts = gen_opts
+        fd, bbox0, corners = _unpack_domain(domain, gen_opts)
+        fh, bbox1, hmin, lsf = _unpack_sizing(edge_length)
+
+        bbox = bbox0 if bbox1 is None else _minmax(bbox0, bbox1)
+        if not isinstance(bbox, tuple):
+            raise ValueError("`bbox` must be a tuple")
+        dim = int(len(bbox) / 2)
+
+        if not np.isscalar(edge_length) and dim == 3:
+            corners = None
+
+        if bbox0 != bbox1 and bbox1 is not None:
+            fd = _Domain(geometry.Rectangle(bbox) if dim == 2 else geometry.Cube(bbox))
+
+        bbox = np.array(bbox).reshape(-1, 2)
+        h0 = hmin if hmin is not None else gen_opts["h0"]
+        if h0 < 0:
+            raise ValueError("`h0` must be > 0")
+
+        self.dim, self.fd, self.h0 = dim, fd, h0
+        self.L0mult = 1 + 0.4 / 2 ** (dim - 1)
+        self.delta_t = gen_opts["delta_t"]
+        self.geps = gen_opts["geps_mult"] * h0
+        self.deps = np.sqrt(np.finfo(np.double).eps) * h0
+
+        self.sizing = _Sizing(edge_length, dim)
+
+        pfix, nfix = _unpack_pfix(dim, gen_opts)
+        if corners is not None:
+            corners = corners[fd(corners) > -1000 * self.deps]
+            pfix = np.append(pfix, corners, axis=0)
+            nfix = len(pfix)
+        print_msg1(f"Constraining {nfix} fixed points...")
+
+        p = _initialize_points(dim, self.geps, bbox, self.sizing, fd, h0, gen_opts, pfix)
+
+        if gen_opts["max_iter"] < 0:
+            raise ValueError("`max_iter` must be > 0")
+        self.max_iter = gen_opts["max_iter"]
+        N_pts = p.shape[0]
+        assert N_pts > 0, "No vertices to mesh with!"
+        print_msg1("Commencing mesh generation with %d vertices on rank %d." % (N_pts, 0))
+
+        levels = [fd]
+        if gen_opts["subdomains"] is not None:
+            for sub in gen_opts["subdomains"]:
+                sfd, _, _ = _unpack_domain(sub, gen_opts)
+                levels.append(sfd)
+        self.levels = levels
+        self.batched = fd.is_batched
+        if self.batched and len(levels) > 1:
+            raise NotImplementedError("subdomains are not supported with a batched-SDF domain")
+        # a host-callable level moves the projection to the host (slow path)
+        self.host_levels = not self.batched and not all(lv.is_program for lv in levels)
+        if self.host_levels:
+            print_msg1("Host-callable domain: the Newton projection runs on the host")
+        self.eng = _Engine(dim, p, nfix)
+        self._lv = None
+
+    @property
+    def capturable(self):
+        """the iteration can run as one host-synchronisation free sequence"""
+        return (not self.batched and not self.host_levels and self.sizing.host is None
+                and self.fd.is_program)
+
+    def iterate(self, count, print_msg2=lambda m: None):
+        eng = self.eng
         eng.triangulate()
-        eng.filter(fd, geps)
-        if count == max_iter - 1:
-            print_msg1("Termination reached...maximum number of iterations reached.")
-            _termination(eng, fd, gen_opts, h0, deps)
-            break
+        eng.filter(self.fd, self.geps)
         eng.build_adjacency()
-        eng.step(sizing, [] if (host_levels or batched) else levels, L0mult, delta_t, h0, deps)
-        if batched:
-            eng.project_batched(fd)
-        elif host_levels:
-            eng.project_host(levels, deps, h0)
-        maxdp = eng.max_movement(delta_t)
+        eng.step(self.sizing, [] if (self.host_levels or self.batched) else self.levels,
+                 self.L0mult, self.delta_t, self.h0, self.deps)
+        if self.batched:
+            eng.project_batched(self.fd)
+        elif self.host_levels:
+            eng.project_host(self.levels, self.deps, self.h0)
+        maxdp = eng.max_movement(self.delta_t)
         print_msg2(
             "Iteration #%d, max movement is %f, there are %d vertices and %d cells"
             % (count + 1, maxdp, eng.n, int(eng.counters[N.CNT_KEPT].item()))
         )
-        assert maxdp < 1000 * h0, "max movement indicates there's a convergence problem"
-        count += 1
-        end = time.time()
-        print_msg2("     Elapsed wall-clock time %f : " % (end - start))
-    return eng.result()
+        assert maxdp < 1000 * self.h0, "max movement indicates there's a convergence problem"
+
+    def iterate_async(self, flags_out):
+        """the checked iteration's kernels on the current stream, with no host
+        synchronisation: points are read from P and the result copied back
+        into P, so a captured graph replays on fixed buffers.  The device
+        flags of the iteration are OR-ed into flags_out (int64[1]); a set
+        flag means the result must be discarded and the iteration redone
+        with iterate()."""
+        eng = self.eng
+        st = D.stream_ptr()
+        if self._lv is None:
+            self._lv = (N.SdfProgram * len(self.levels))()
+            for i, L in enumerate(self.levels):
+                self._lv[i] = L.program().struct
+        N.call("dm_delaunay", self.dim, D.ptr(eng.P), eng.n, D.ptr(eng.cells), eng.cap_cells,
+               D.ptr(eng.counters), D.ptr(eng.ws_dt), eng.ws_dt.numel(), st)
+        N.call("dm_filter_cells", self.dim, D.ptr(eng.P), D.ptr(eng.cells), eng.cap_cells,
+               self.fd.program().struct, self.geps, D.ptr(eng.kept), D.ptr(eng.counters), None,
+               0, st)
+        eng.adjacency_async()
+        N.call("dm_bar_sums", self.dim, D.ptr(eng.P), eng.n, D.ptr(eng.adj), eng.adj_cap,
+               D.ptr(eng.deg), self.sizing.struct, D.ptr(eng.partials), st)
+        N.call("dm_update_points", self.dim, D.ptr(eng.P), D.ptr(eng.P2), eng.n, D.ptr(eng.adj),
+               eng.adj_cap, D.ptr(eng.deg), self.sizing.struct, D.ptr(eng.partials), self.L0mult,
+               self.delta_t, eng.nfix, self._lv, len(self.levels), self.h0, self.deps,
+               D.ptr(eng.maxf), eng.grid_exp, st)
+        eng.P.copy_(eng.P2)
+        torch.bitwise_or(flags_out, eng.counters[N.CNT_FLAGS:N.CNT_FLAGS + 1], out=flags_out)
+
+    def finish(self, print_msg1=lambda m: None):
+        eng = self.eng
+        eng.triangulate()
+        eng.filter(self.fd, self.geps)
+        print_msg1("Termination reached...maximum number of iterations reached.")
+        _termination(eng, self.fd, self.opts, self.h0, self.deps)
 
 
 def _termination(eng, fd, opts, h0, deps, sliver=False):

@@ -43,6 +43,7 @@ def main():
         "engine": "reference loop (SeismicMesh generation/mesh_generator.py) with Qhull standing in for CGAL",
         "n_points": int(len(p)), "n_cells": int(len(t)),
         "min_quality": float(q.min()), "mean_quality": float(q.mean()),
+        "quality_q001": float(np.quantile(q, 0.001)), "quality_q01": float(np.quantile(q, 0.01)),
         "area": float(np.abs(SM.geometry.simp_vol(p, t)).sum()),
         "size_min": float(np.min(ef.cell_size.values) if hasattr(ef.cell_size, "values") else 0.0),
         "sizing_s": t1 - t0, "generate_mesh_s": t2 - t1,
