@@ -5,10 +5,11 @@ tests assert (where they assert) and the counts of the reference itself run
 through the oracle harness (tests/golden/make_golden.py gradient reftests2);
 the decoded velocity fixtures are stored as arrays, not as the files.
 
-Tolerances: the reference tests use atol=100 on vertex and cell counts.  The
-triangulations differ only on the degenerate initial lattice (tie-breaking)
-and through float32 positions, so counts must agree with the reference run
-within max(100, 1.5%)."""
+Tolerances: the reference tests use atol=100 on vertex and cell counts;
+here counts must agree with the reference run within 1 % (the generation
+tolerance of the configurations).  The triangulations differ only on the
+degenerate initial lattice (tie-breaking) and through float32 positions.
+Every comparison prints its relative difference."""
 import json
 import os
 
@@ -25,8 +26,10 @@ pytestmark = pytest.mark.gpu
 REFT = json.load(open(os.path.join(GOLDEN, "reference_tests2.json")))
 
 
-def _close(got, want, rel=0.015, atol=100):
-    return all(abs(g - w) <= max(atol, rel * w) for g, w in zip(got, want))
+def _close(got, want, rel=0.01):
+    for g, w in zip(got, want):
+        print(f"count: gpu {g} reference {w} rel {(g - w) / w:+.3e}")
+    return all(abs(g - w) <= rel * w for g, w in zip(got, want))
 
 
 @pytest.mark.parametrize("case", ["g2", "g2w", "g3"])
