@@ -368,15 +368,21 @@ int mlp_eval_fp32(const dm_mlp *mp, const float *pts, int stride, int64_t n, flo
 // ---------------------------------------------------------------------------
 // inference: tcgen05 (cta_group::1, kind::f16), M = N = 128, K = 16 per MMA.
 //
+// One persistent CTA per SM with two warpgroups.  Each warpgroup owns a
+// tile of 128 points at a time, its activation tiles and a 128-column FP32
+// accumulator in tensor memory, and runs features -> 4 x (MMAs, epilogue)
+// on its own; the tensor core executes one group's MMAs while the other
+// group is in its epilogue.
+//
 // Shared memory (1024-aligned), all operand tiles K-major with the 128-byte
 // swizzle: a tile is 128 rows x 64 BF16 (128 B per row, 8-row groups of
 // 1024 B, 16-byte chunk j of row r stored at chunk j ^ (r & 7)), which is
 // what a TMA load with CU_TENSOR_MAP_SWIZZLE_128B writes.
-//   W1: 1 tile; W2..W4: 2 tiles each (K = 0..63, 64..127); A: 2 tiles
-//   (activations of the current layer; layer 1 uses the first).
-// Tensor memory: one 128-lane x 128-column FP32 accumulator; lane r = row r
-// (point r of the tile), column j = output feature j.  Warp w reads lanes
-// 32w..32w+31.
+//   W1: 1 tile; W2..W4: 2 tiles each (K = 0..63, 64..127); per group, A: 2
+//   tiles (activations of the current layer; layer 1 uses the first).
+// Tensor memory: 256 columns; group g's accumulator is columns 128 g..,
+// lane r = row r (point r of its tile), column j = output feature j.  Warp w
+// of a group reads lanes 32 (w mod 4)...
 constexpr int kTile = 128;
 constexpr int kTileBytes = 128 * 128;  // 128 rows x 128 B
 constexpr uint32_t kIdesc = (1u << 4)            // D: FP32
@@ -393,14 +399,14 @@ static __device__ int g_mlp_err;
 struct TcSmem {
   uint8_t w1[kTileBytes];
   uint8_t w[3][2][kTileBytes];
-  uint8_t a[2][kTileBytes];
+  uint8_t a[2][2][kTileBytes];  // [group][K half]
   float bias[4][kW];
   float w5[kW];
   float b5;
   int err;
   uint32_t tmem;
   uint64_t bar_w;
-  uint64_t bar_mma;
+  uint64_t bar_mma[2];
 };
 constexpr size_t kTcSmemBytes = sizeof(TcSmem) + 1024;
 
@@ -439,6 +445,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   }
 }
 
+// barrier of one warpgroup (named barrier 1 + g, 128 threads) that also
+// returns whether v holds for all of its threads
+__device__ __forceinline__ bool group_and(bool v, int g) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, 128, p;\n"
+      " selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(1 + g)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void group_sync(int g) {
+  asm volatile("bar.sync %0, 128;\n" ::"r"(1 + g) : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   uint32_t r[32];
   asm volatile(
@@ -462,10 +484,10 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
 }
 
 // 8 BF16 values (16 bytes) into chunk j (0..15 over K = 0..127) of row r of
-// the activation tiles
-__device__ __forceinline__ void st_chunk(TcSmem &S, int r, int j, const float *v8) {
+// group g's activation tiles
+__device__ __forceinline__ void st_chunk(TcSmem &S, int g, int r, int j, const float *v8) {
   const int tile = j >> 3, cj = j & 7;
-  uint8_t *p = S.a[tile] + r * 128 + ((cj ^ (r & 7)) << 4);
+  uint8_t *p = S.a[g][tile] + r * 128 + ((cj ^ (r & 7)) << 4);
   uint4 q = make_uint4(pack_bf16(v8[0], v8[1]), pack_bf16(v8[2], v8[3]),
                        pack_bf16(v8[4], v8[5]), pack_bf16(v8[6], v8[7]));
   *reinterpret_cast<uint4 *>(p) = q;
@@ -489,7 +511,7 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t adesc, uint64_t
       : "memory");
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     k_mlp_infer_tc(const __grid_constant__ CUtensorMap tw1, const __grid_constant__ CUtensorMap tw2,
                    const __grid_constant__ CUtensorMap tw3, const __grid_constant__ CUtensorMap tw4,
                    MlpDev m, const float *__restrict__ pts, int stride, int64_t n,
@@ -498,16 +520,18 @@ __global__ void __launch_bounds__(128, 1)
   TcSmem &S = *reinterpret_cast<TcSmem *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int g = warp >> 2, r = tid & 127;  // warpgroup, row of its tile
   const int64_t ntiles = (n + kTile - 1) / kTile;
 
   if (tid == 0) {
     S.err = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.bar_w)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.bar_mma)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.bar_mma[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&S.bar_mma[1])));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 0) {  // tensor memory: 128 columns
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(
+  if (warp == 0) {  // tensor memory: 2 x 128 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;\n" ::"r"(
         smem_u32(&S.tmem)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
@@ -518,7 +542,7 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = S.tmem;
+  const uint32_t tmem = S.tmem + (uint32_t)(g * 128);  // this group's accumulator
 
   if (tid == 0) {  // the weights, once per CTA (7 TMA tiles of 16 KB)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
@@ -532,14 +556,15 @@ __global__ void __launch_bounds__(128, 1)
       tma_load_2d(S.w[l][1], maps[l], 64, 0, &S.bar_w);
     }
   }
-  // every decision that ends a loop is taken by the whole CTA
   bool ok = __syncthreads_and(mbar_wait(&S.bar_w, 0));
   uint32_t phase = 0;
   bool mma_pending = false;
 
-  for (int64_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+  // every decision that ends a loop is taken by the whole warpgroup
+  for (int64_t tile = 2 * (int64_t)blockIdx.x + g; ok && tile < ntiles;
+       tile += 2 * (int64_t)gridDim.x) {
     // layer-1 input: Fourier features of point r of the tile
-    const int64_t row = tile * kTile + tid;
+    const int64_t row = tile * kTile + r;
     float xp[3] = {0.f, 0.f, 0.f};
     if (row < n) {
       const float *x = pts + row * stride;
@@ -550,45 +575,45 @@ __global__ void __launch_bounds__(128, 1)
     for (int j = 0; j < 4; ++j) {  // chunks 0..3: sin, 4..7: cos
       float sv[8], cv[8];
       for (int q = 0; q < 8; ++q) fourier(m, xp, 8 * j + q, &sv[q], &cv[q]);
-      st_chunk(S, tid, j, sv);
-      st_chunk(S, tid, 4 + j, cv);
+      st_chunk(S, g, r, j, sv);
+      st_chunk(S, g, r, 4 + j, cv);
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
+    group_sync(g);
 
     for (int l = 0; l < 4 && ok; ++l) {
-      if (tid == 0) {
+      if (r == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const int nk = kK(l) / 16;
         for (int k = 0; k < nk; ++k) {
           const int t = k >> 2, off = (k & 3) * 32;
           const uint8_t *btile = l == 0 ? S.w1 : S.w[l - 1][t];
-          mma_bf16(tmem, sw128_desc(smem_u32(S.a[t]) + off), sw128_desc(smem_u32(btile) + off),
-                   k > 0);
+          mma_bf16(tmem, sw128_desc(smem_u32(S.a[g][t]) + off),
+                   sw128_desc(smem_u32(btile) + off), k > 0);
         }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                smem_u32(&S.bar_mma))
+                smem_u32(&S.bar_mma[g]))
             : "memory");
       }
       mma_pending = true;
-      ok = __syncthreads_and(mbar_wait(&S.bar_mma, phase));
+      ok = group_and(mbar_wait(&S.bar_mma[g], phase), g);
       if (!ok) break;
       mma_pending = false;
       phase ^= 1;
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+      const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
       if (l < 3) {
         for (int c0 = 0; c0 < kW; c0 += 32) {
           float v[32];
           tmem_ld32(taddr + c0, v);
           for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + S.bias[l][c0 + i], 0.f);
-          for (int j = 0; j < 4; ++j) st_chunk(S, tid, (c0 >> 3) + j, v + 8 * j);
+          for (int j = 0; j < 4; ++j) st_chunk(S, g, r, (c0 >> 3) + j, v + 8 * j);
         }
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
+        group_sync(g);
       } else {
         float acc = S.b5;
         for (int c0 = 0; c0 < kW; c0 += 32) {
@@ -599,19 +624,19 @@ __global__ void __launch_bounds__(128, 1)
         }
         if (row < n) dout[row] = m.out_scale * acc;
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
+        group_sync(g);
       }
     }
   }
   if (!ok) {
-    if (tid == 0) atomicExch(&g_mlp_err, 1);
-    if (mma_pending) mbar_wait(&S.bar_mma, phase);  // bounded: let an issued MMA drain
+    if (r == 0) atomicExch(&g_mlp_err, 1);
+    if (mma_pending) mbar_wait(&S.bar_mma[g], phase);  // bounded: let an issued MMA drain
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;\n" ::"r"(S.tmem));
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -683,9 +708,9 @@ int mlp_eval_tc(const dm_mlp *mp, const float *pts, int stride, int64_t n, float
   const MlpDev m = to_dev(mp);
   int sms = 0;
   DM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t ntiles = (n + kTile - 1) / kTile;
-  const int grid = (int)(ntiles < sms ? ntiles : sms);
-  k_mlp_infer_tc<<<grid, 128, kTcSmemBytes, s>>>(maps[0], maps[1], maps[2], maps[3], m, pts,
+  const int64_t npairs = (n + 2 * kTile - 1) / (2 * kTile);
+  const int grid = (int)(npairs < sms ? npairs : sms);
+  k_mlp_infer_tc<<<grid, 256, kTcSmemBytes, s>>>(maps[0], maps[1], maps[2], maps[3], m, pts,
                                                  stride, n, d);
   note_launches(1);
   DM_LAUNCH_CHECK();
