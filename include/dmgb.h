@@ -417,7 +417,8 @@ typedef struct dm_iso {
 } dm_iso;
 /* triangle count of the surface: rowstart int32[2*(n0-1)*(n1-1) + 1]
  * receives the exclusive scan of the per-row counts in its first
- * (n0-1)*(n1-1) + 1 entries; tmp holds >= (n0-1)*(n1-1)/1024 + 16 ints.
+ * (n0-1)*(n1-1) + 1 entries; tmp holds >= 2 (R/1024 + 3) + R/2^20 + 17 ints
+ * for R = (n0-1)*(n1-1) rows.
  * Synchronises the stream. */
 int dm_iso_count(const dm_iso *iso, int32_t *rowstart, int32_t *tmp,
                  int64_t *ntri_host, void *stream);

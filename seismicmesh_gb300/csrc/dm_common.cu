@@ -108,13 +108,25 @@ int exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
                        int32_t *tmp, cudaStream_t s) {
   int64_t nb = (n + 1023) / 1024;
   if (nb < 1) nb = 1;
-  if (nb > 4096) {
-    set_error("exclusive_scan_i32: n=%lld exceeds 4M", (long long)n);
+  if (nb <= 4096) {
+    k_scan_reduce<<<(int)nb, 256, 0, s>>>(in, n, tmp);
+    k_scan_bsums<<<1, 1024, 0, s>>>(tmp, (int)nb);
+    k_scan_apply<<<(int)nb, 256, 0, s>>>(in, out, n, tmp, (int)nb);
+    DM_LAUNCH_CHECK();
+    return DM_OK;
+  }
+  // two levels: the block sums are scanned like the input
+  const int64_t nb2 = (nb + 1023) / 1024;
+  if (nb2 > 4096) {
+    set_error("exclusive_scan_i32: n=%lld exceeds 2^32", (long long)n);
     return DM_ERR_CAPACITY;
   }
-  k_scan_reduce<<<(int)nb, 256, 0, s>>>(in, n, tmp);
-  k_scan_bsums<<<1, 1024, 0, s>>>(tmp, (int)nb);
-  k_scan_apply<<<(int)nb, 256, 0, s>>>(in, out, n, tmp, (int)nb);
+  int32_t *b1 = tmp, *b1x = tmp + nb + 1, *b2 = b1x + nb + 1;
+  k_scan_reduce<<<(int)nb, 256, 0, s>>>(in, n, b1);
+  k_scan_reduce<<<(int)nb2, 256, 0, s>>>(b1, nb, b2);
+  k_scan_bsums<<<1, 1024, 0, s>>>(b2, (int)nb2);
+  k_scan_apply<<<(int)nb2, 256, 0, s>>>(b1, b1x, nb, b2, (int)nb2);
+  k_scan_apply<<<(int)nb, 256, 0, s>>>(in, out, n, b1x, (int)nb);
   DM_LAUNCH_CHECK();
   return DM_OK;
 }

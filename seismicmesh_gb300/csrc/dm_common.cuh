@@ -97,9 +97,13 @@ __device__ __forceinline__ int64_t warp_append(int64_t *ctr, bool want) {
   return base + __popc(m & ((1u << lane) - 1));
 }
 
-// Exclusive scan of int32 counts (n <= 4M) into out[0..n]; out[n] = total.
-// tmp must hold >= scan_tmp_elems(n) ints.
-inline int64_t scan_tmp_elems(int64_t n) { return (n + 1023) / 1024 + 16; }
+// Exclusive scan of int32 counts (n < 2^32) into out[0..n]; out[n] = total.
+// tmp must hold >= scan_tmp_elems(n) ints (block sums, and above 4M
+// elements their scan and a second level of sums).
+inline int64_t scan_tmp_elems(int64_t n) {
+  const int64_t nb = (n + 1023) / 1024 + 1;
+  return 2 * (nb + 1) + (nb + 1023) / 1024 + 16;
+}
 int exclusive_scan_i32(const int32_t *in, int32_t *out, int64_t n,
                        int32_t *tmp, cudaStream_t s);
 

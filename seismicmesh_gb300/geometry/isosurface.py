@@ -54,7 +54,8 @@ class Isosurface:
             iso.h[k] = (bbox[2 * k + 1] - bbox[2 * k]) / (n[k] - 1)
         nrow = (n[0] - 1) * (n[1] - 1)
         rowstart = D.empty((2 * nrow + 1,), torch.int32)
-        tmp = D.empty((nrow // 1024 + 32,), torch.int32)
+        nb = nrow // 1024 + 2
+        tmp = D.empty((2 * (nb + 1) + nb // 1024 + 32,), torch.int32)
         ntri = N.c_i64(0)
         N.call("dm_iso_count", iso, D.ptr(rowstart), D.ptr(tmp), ntri, D.stream_ptr())
         self.ntri = int(ntri.value)

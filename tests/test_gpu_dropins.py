@@ -62,3 +62,14 @@ def test_unique_edges_with_hub_vertices(cuda, hub_degree):
     got = sm.geometry.unique_edges(e)
     ref = np.unique(np.sort(e, axis=1), axis=0)
     np.testing.assert_array_equal(got, ref)
+
+
+def test_unique_edges_above_four_million_vertices(cuda):
+    """n = 5e6 vertex buckets: the bucket scan takes its two-level path"""
+    rng = np.random.default_rng(9)
+    n = 5_000_000
+    e = rng.integers(0, n, size=(1_000_000, 2)).astype(np.int32)
+    e[0] = (n - 1, 0)
+    got = sm.geometry.unique_edges(e)
+    ref = np.unique(np.sort(e, axis=1), axis=0)
+    np.testing.assert_array_equal(got, ref)

@@ -87,3 +87,24 @@ def test_gmsh22_writer_roundtrip(tmp_path):
         pp, tt = read_gmsh22(str(f))
         np.testing.assert_array_equal(pp[:, :dim], p)
         np.testing.assert_array_equal(tt, t)
+
+
+def test_ibm_float_known_answers():
+    """IBM System/360 single-precision words with known values, written from
+    the format's definition (sign bit, 7-bit excess-64 base-16 exponent,
+    24-bit fraction): decoded independently of this file's encoder"""
+    from seismicmesh_gb300.sizing.mesh_size_function import _ibm_to_ieee
+
+    words = np.array([
+        0x00000000,  # 0
+        0x41100000,  # 16^1 * 1/16 = 1.0
+        0xC1100000,  # -1.0
+        0x42640000,  # 16^2 * 0x64/256 = 100.0
+        0xC276A000,  # -(16^2 * 0x76A000/2^24) = -118.625
+        0x43A98000,  # 16^3 * 0xA98000/2^24 = 2712.0 (a velocity)
+        0x40800000,  # 16^0 * 0.5 = 0.5
+        0x3F200000,  # 16^-1 * 0.125 = 0.0078125
+    ], dtype=">u4")
+    want = np.array([0.0, 1.0, -1.0, 100.0, -118.625, 2712.0, 0.5, 0.0078125])
+    got = np.asarray(_ibm_to_ieee(words), dtype=np.float64).ravel()
+    np.testing.assert_array_equal(got, want)
