@@ -1825,6 +1825,117 @@ __device__ __forceinline__ int cheb3(const int *cc, int x, int y, int z) {
   return max(abs(x - cc[0]), max(abs(y - cc[1]), abs(z - cc[2])));
 }
 
+// Every point of each lane's range [off, off + len) of pts, visited by the
+// whole warp: an inclusive prefix sum flattens the 32 ranges and each lane
+// takes one point at a time (a binary search over the prefix finds its
+// range).  A warp whose hits are few and uneven keeps all lanes busy, and
+// the point loads are independent.
+template <typename F>
+__device__ __forceinline__ void warp_ranges(const float4 *pts, int off, int len, int lane, F f) {
+  int incl = len;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int base = off - (incl - len);  // point t of the flat list is pts[base_r + t]
+  for (int t0 = 0; t0 < total; t0 += 32) {
+    const int t = t0 + lane;
+    int r = 0;  // first range whose inclusive sum exceeds t
+    for (int s = 16; s; s >>= 1)
+      if (__shfl_sync(0xffffffffu, incl, r + s - 1) <= t) r += s;
+    const int b = __shfl_sync(0xffffffffu, base, r);
+    if (t < total) f(pts[b + t]);
+  }
+}
+
+// Box of the cell row x0 <= x < x1 at (y, z), padded for the rounding of the
+// cell assignment (floor((x - lo) / cs) in FP32 may place a point a few
+// ulps of the grid extent outside its cell's nominal box).
+__device__ __forceinline__ void row_box3(const GridParams &g, int x0, int x1, int y, int z,
+                                         float *lo, float *hi) {
+  const int c0[3] = {x0, y, z}, c1[3] = {x1, y + 1, z + 1};
+  for (int k = 0; k < 3; ++k) {
+    const float pad = (fabsf(g.lo[k]) + (float)g.dims[k] * g.cs) * 1e-6f;
+    lo[k] = g.lo[k] + (float)c0[k] * g.cs - pad;
+    hi[k] = g.lo[k] + (float)c1[k] * g.cs + pad;
+  }
+}
+
+// The points of coarse blocks b0 and b1 (b1 < 0: none) that may lie in the
+// region, visited by the whole warp: lane l holds cell row l % 16 (the 4
+// cells along x at one (y, z)) of block l < 16 ? b0 : b1.  A row whose box
+// misses the region, or whose cells all lie within Chebyshev distance rex of
+// cell cc (already scanned), is dropped; a point in such a cell is skipped.
+constexpr int kBs3 = 4;  // coarse block edge in 3D (GridParams::bs)
+template <typename F>
+__device__ __forceinline__ void scan_block_pair3(const DTArgs &A, const GridParams &g,
+                                                 const Region3 &R, int b0, int b1,
+                                                 const int *cc, int rex, int lane, F f) {
+  const int b = lane < 16 ? b0 : b1, r = lane & 15;
+  int off = 0, len = 0;
+  if (b >= 0) {
+    const int bxi = b % g.bdims[0], byi = (b / g.bdims[0]) % g.bdims[1],
+              bzi = b / (g.bdims[0] * g.bdims[1]);
+    const int y = byi * kBs3 + (r & 3), z = bzi * kBs3 + (r >> 2);
+    const int x0 = bxi * kBs3, x1 = min(x0 + kBs3, g.dims[0]);
+    const bool done = abs(y - cc[1]) <= rex && abs(z - cc[2]) <= rex && x0 >= cc[0] - rex &&
+                      x1 - 1 <= cc[0] + rex;
+    if (y < g.dims[1] && z < g.dims[2] && !done) {
+      float lo[3], hi[3];
+      row_box3(g, x0, x1, y, z, lo, hi);
+      if (region_hits3(R, lo, hi)) {
+        const int c0 = x0 + g.dims[0] * (y + g.dims[1] * z);
+        off = A.cell_start[c0];
+        len = A.cell_start[c0 + (x1 - x0)] - off;
+      }
+    }
+  }
+  warp_ranges(A.spts, off, len, lane, [&](float4 q) {
+    const int j = __float_as_int(q.w);
+    if (j < 0) return;  // duplicate
+    if (cheb3(cc, cell_coord(g, q.x, 0), cell_coord(g, q.y, 1), cell_coord(g, q.z, 2)) <= rex)
+      return;
+    f(j, q);
+  });
+}
+
+// Every point of the coarse blocks [blo, bhi] (block coordinates) whose
+// tight box meets the region: lanes test 32 blocks at a time and the hits
+// are scanned two by two by the whole warp.
+template <typename F>
+__device__ __forceinline__ void scan_blocks3(const DTArgs &A, const GridParams &g,
+                                             const Region3 &R, const int *blo, const int *bhi,
+                                             const int *cc, int rex, int lane, F f) {
+  const int sx = bhi[0] - blo[0] + 1, sy = bhi[1] - blo[1] + 1, sz = bhi[2] - blo[2] + 1;
+  if (sx <= 0 || sy <= 0 || sz <= 0) return;
+  const int64_t nb = (int64_t)sx * sy * sz;
+  int pending = -1;  // a hit block waiting for a partner (warp-uniform)
+  for (int64_t t0 = 0; t0 < nb; t0 += 32) {
+    const int64_t t = t0 + lane;
+    int bid = -1;
+    if (t < nb) {
+      const int bxi = blo[0] + (int)(t % sx), byi = blo[1] + (int)((t / sx) % sy),
+                bzi = blo[2] + (int)(t / ((int64_t)sx * sy));
+      bid = bxi + g.bdims[0] * (byi + g.bdims[1] * bzi);
+      if (A.blk_cnt[bid] == 0 || !region_hits3(R, A.blk_box + 6 * bid, A.blk_box + 6 * bid + 3))
+        bid = -1;
+    }
+    unsigned m = __ballot_sync(0xffffffffu, bid >= 0);
+    while (m) {
+      const int h = __shfl_sync(0xffffffffu, bid, __ffs(m) - 1);
+      m &= m - 1;
+      if (pending < 0) {
+        pending = h;
+        continue;
+      }
+      scan_block_pair3(A, g, R, pending, h, cc, rex, lane, f);
+      pending = -1;
+    }
+  }
+  if (pending >= 0) scan_block_pair3(A, g, R, pending, -1, cc, rex, lane, f);
+}
+
 // exhaustive gift-wrap query on face (p, a, b), 3D
 __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
                                    int ia, int ib, int lane, int &ovf,
@@ -1876,15 +1987,19 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     make_region3(H, F.p, a, b, n, nn, la, lb, nullptr);
     region3_floats(H);
     const int ntab = *A.o_ntab;
-    for (int e = lane; e < ntab; e += 32) {
-      const float4 t0 = A.o_tab[2 * e], t1 = A.o_tab[2 * e + 1];
-      const float blo[3] = {t0.x, t0.y, t0.z}, bhi[3] = {t1.x, t1.y, t1.z};
-      if (!region_hits3(H, blo, bhi)) continue;
-      const int s0 = __float_as_int(t0.w), s1 = s0 + __float_as_int(t1.w);
-      for (int i = s0; i < s1; ++i) {
-        const float4 q = A.o_pts[i];
-        consider3(A, F, __float_as_int(q.w), q, best, bx, ovf, W);
+    for (int e0 = 0; e0 < ntab; e0 += 32) {
+      const int e = e0 + lane;
+      int s0 = 0, cnt = 0;
+      if (e < ntab) {
+        const float4 t0 = A.o_tab[2 * e], t1 = A.o_tab[2 * e + 1];
+        const float blo[3] = {t0.x, t0.y, t0.z}, bhi[3] = {t1.x, t1.y, t1.z};
+        if (region_hits3(H, blo, bhi)) {
+          s0 = __float_as_int(t0.w);
+          cnt = __float_as_int(t1.w);
+        }
       }
+      warp_ranges(A.o_pts, s0, cnt, lane,
+                  [&](float4 q) { consider3(A, F, __float_as_int(q.w), q, best, bx, ovf, W); });
     }
     best = tourney3(A, F, best, ovf, W);
     if (best >= 0)
@@ -1947,52 +2062,27 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
       for (int t = lane; t < ncell; t += 32) {
         int x = lo[0] + t % sx, y = lo[1] + (t / sx) % sy, z = lo[2] + t / (sx * sy);
         if (cheb3(cc, x, y, z) <= rex) continue;
-        float blo[3] = {g.lo[0] + x * g.cs, g.lo[1] + y * g.cs, g.lo[2] + z * g.cs};
-        float bhi[3] = {blo[0] + g.cs, blo[1] + g.cs, blo[2] + g.cs};
+        float blo[3], bhi[3];
+        row_box3(g, x, x + 1, y, z, blo, bhi);
         if (!region_hits3(R, blo, bhi)) continue;
         for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
                  [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
       }
     } else {
       int blo[3], bhi[3];
-      int64_t nb = 1;
       for (int k = 0; k < 3; ++k) {
-        blo[k] = lo[k] / g.bs;
-        bhi[k] = hi[k] / g.bs;
-        nb *= (bhi[k] - blo[k] + 1);
+        blo[k] = lo[k] / kBs3;
+        bhi[k] = hi[k] / kBs3;
       }
-      int sx = bhi[0] - blo[0] + 1, sy = bhi[1] - blo[1] + 1;
-      for (int64_t t = lane; t < nb; t += 32) {
-        int bxi = blo[0] + (int)(t % sx), byi = blo[1] + (int)((t / sx) % sy),
-            bzi = blo[2] + (int)(t / (sx * sy));
-        int bid = bxi + g.bdims[0] * (byi + g.bdims[1] * bzi);
-        if (A.blk_cnt[bid] == 0) continue;
-        if (!region_hits3(R, A.blk_box + 6 * bid, A.blk_box + 6 * bid + 3)) continue;
-        for (int z = bzi * g.bs; z < min(bzi * g.bs + g.bs, g.dims[2]); ++z)
-          for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
-            for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
-              if (cheb3(cc, x, y, z) <= rex) continue;
-              for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                       [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
-            }
-      }
+      scan_blocks3(A, g, R, blo, bhi, cc, rex, lane,
+                   [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
     }
   } else {
     // every block that may hold a point on the positive side
     if (lane == 0) L2S_ADD(1, 1);
-    for (int bid = lane; bid < g.nblocks; bid += 32) {
-      if (A.blk_cnt[bid] == 0) continue;
-      if (!region_hits3(R, A.blk_box + 6 * bid, A.blk_box + 6 * bid + 3)) continue;
-      int bxi = bid % g.bdims[0], byi = (bid / g.bdims[0]) % g.bdims[1],
-          bzi = bid / (g.bdims[0] * g.bdims[1]);
-      for (int z = bzi * g.bs; z < min(bzi * g.bs + g.bs, g.dims[2]); ++z)
-        for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
-          for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
-            if (cheb3(cc, x, y, z) <= rex) continue;
-            for_cell(A, x + g.dims[0] * (y + g.dims[1] * z),
-                     [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
-          }
-    }
+    const int blo[3] = {0, 0, 0}, bhi[3] = {g.bdims[0] - 1, g.bdims[1] - 1, g.bdims[2] - 1};
+    scan_blocks3(A, g, R, blo, bhi, cc, rex, lane,
+                 [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
   }
   best = tourney3(A, F, best, ovf, W);
 #ifdef DM_L2_STATS
