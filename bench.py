@@ -703,7 +703,9 @@ def ncu_case(args):
           iterations, then one more full iteration (triangulation, filter,
           adjacency, bar sums, update): the launches an ncu capture selects.
     mlp:  the salt body's network trained briefly, then dm_mlp_eval on 2^22
-          points uniform in the box, args.warmup + 1 times."""
+          points uniform in the box, args.warmup + 1 times.
+    salt: the salt body with its exact isosurface SDF (h0 = hmin = 50 m) for
+          args.warmup DistMesh iterations, then one more triangulation."""
     import torch
 
     import seismicmesh_gb300 as sm
@@ -730,6 +732,34 @@ def ncu_case(args):
             nn.mlp_eval_device(X, 4, n, d)
         torch.cuda.synchronize()
         print("ncu case done:", n, "points", flush=True)
+        return
+    if args.ncu_case == "salt":
+        import contextlib
+
+        from seismicmesh_gb300 import synthetic as S
+
+        with contextlib.redirect_stdout(sys.stderr):
+            vp, B, bbox = S.salt_model_3d()
+            ef = sm.get_sizing_function_from_segy(None, bbox, velocity_data=vp, nz=vp.shape[0],
+                                                  nx=vp.shape[1], ny=vp.shape[2], **SALT)
+            iso = sm.Isosurface(B, bbox, 0.5)
+        h0 = SALT["hmin"]
+        fd = MG._Domain(iso)
+        sizing = MG._Sizing(ef, 3)
+        opts = {"points": None, "r0m_is_h0": False, "seed": 0}
+        p0 = MG._initialize_points(3, 0.1 * h0, np.array(bbox).reshape(-1, 2), sizing, fd, h0, opts,
+                                   np.empty((0, 3)))
+        eng = MG._Engine(3, p0, 0)
+        deps = float(np.sqrt(np.finfo(float).eps) * h0)
+        for _ in range(args.warmup):
+            eng.triangulate()
+            eng.filter(fd, 0.1 * h0)
+            eng.build_adjacency()
+            eng.step(sizing, [], 1.1, 0.30, h0, deps)
+            eng.project_batched(fd)
+        eng.triangulate()
+        torch.cuda.synchronize()
+        print("ncu case done:", eng.n, "points", int(eng.counters_host()[0]), "cells", flush=True)
         return
     ball = sm.Ball([0.0, 0.0, 0.0], 1.0)
     fd = MG._Domain(ball)
@@ -764,10 +794,11 @@ def main():
                          "and print its JSON object")
     ap.add_argument("--salt-only", action="store_true",
                     help="run only the salt-body workload and print its JSON object")
-    ap.add_argument("--ncu-case", choices=["ball", "mlp"], default=None,
+    ap.add_argument("--ncu-case", choices=["ball", "mlp", "salt"], default=None,
                     help="profiling case: ball (the bench workload for --warmup iterations, then "
-                         "one more) or mlp (tensor-core inference on 2^22 points); no timing, "
-                         "no JSON line")
+                         "one more), mlp (tensor-core inference on 2^22 points) or salt (the salt "
+                         "body, exact SDF, --warmup iterations, then one triangulation); no "
+                         "timing, no JSON line")
     args = ap.parse_args()
     if args.ncu_case:
         ncu_case(args)

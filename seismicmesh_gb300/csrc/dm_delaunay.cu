@@ -1553,18 +1553,61 @@ __device__ __forceinline__ void ldp(const DTArgs &A, int i, float *x) {
 // 3D: compare candidate j against current best on face (p,a,b)
 struct Face3 {
   int ip, ia, ib;
+  int gfix;  // GridParams::gfix (the exact stages rebuild their frame from it)
   float p[3], a[3], b[3];
   float V[3], U[3];
-  FxFrame fr;    // fixed-point frame at p covering 8x the face size
-  int4 IA, IB;   // a, b in that frame
 };
 
-__device__ __forceinline__ void face3_frame(Face3 &F, int gfix) {
+__device__ __forceinline__ void face3_frame(Face3 &F, int gfix) { F.gfix = gfix; }
+
+// Exact stages of the face predicates.  They run only when the FP32 filter
+// cannot decide, so they are compiled once, out of line, and take scalars
+// (the face stays in registers at every inlined filter).  The fixed-point
+// frame is the one at p covering 8x the face size (its largest coordinate
+// difference), in which a and b and the query points are exact or flagged.
+struct FaceFx {
+  FxFrame fr;
+  int4 IA, IB;
+};
+
+__device__ __forceinline__ void face_fx(FaceFx &X, const float *p, const float *a,
+                                        const float *b, int gfix) {
   float e = 0.f;
-  for (int k = 0; k < 3; ++k) e = fmaxf(e, fmaxf(fabsf(F.V[k]), fabsf(F.U[k])));
-  fx_frame<3>(F.fr, F.p, 8.f * e, gfix);
-  F.IA = fx_point<3>(F.fr, F.a);
-  F.IB = fx_point<3>(F.fr, F.b);
+  for (int k = 0; k < 3; ++k) e = fmaxf(e, fmaxf(fabsf(a[k] - p[k]), fabsf(b[k] - p[k])));
+  fx_frame<3>(X.fr, p, 8.f * e, gfix);
+  X.IA = fx_point<3>(X.fr, a);
+  X.IB = fx_point<3>(X.fr, b);
+}
+
+static __device__ __noinline__ int side3_exact(float p0, float p1, float p2, float a0, float a1,
+                                               float a2, float b0, float b1, float b2, float y0,
+                                               float y1, float y2, int gfix,
+                                               dmp::ExactScratch *W) {
+  const float p[3] = {p0, p1, p2}, a[3] = {a0, a1, a2}, b[3] = {b0, b1, b2}, y[3] = {y0, y1, y2};
+  FaceFx X;
+  face_fx(X, p, a, b, gfix);
+  const int4 IY = fx_point<3>(X.fr, y);
+  if (X.IA.w & X.IB.w & IY.w) return dmp::orient3_fx(X.IA, X.IB, IY);
+  return dmp::orient3_slow(p, a, b, y, W);
+}
+
+// perturbed insph3(p, a, b, c, d): the sign in bits 0-1 (sign + 1), bit 2
+// set when an expansion overflowed
+static __device__ __noinline__ int insph_face3_exact(float p0, float p1, float p2, float a0,
+                                                     float a1, float a2, float b0, float b1,
+                                                     float b2, float c0, float c1, float c2,
+                                                     float d0, float d1, float d2, int gfix,
+                                                     dmp::ExactScratch *W) {
+  const float p[3] = {p0, p1, p2}, a[3] = {a0, a1, a2}, b[3] = {b0, b1, b2};
+  const float c[3] = {c0, c1, c2}, d[3] = {d0, d1, d2};
+  FaceFx X;
+  face_fx(X, p, a, b, gfix);
+  const int4 IC = fx_point<3>(X.fr, c), ID = fx_point<3>(X.fr, d);
+  if (X.IA.w & X.IB.w & IC.w & ID.w) return dmp::insph3_fx_sos(X.IA, X.IB, IC, ID) + 1;
+  int ovf = 0;
+  int s = dmp::insph3_slow(p, a, b, c, d, &ovf, W);
+  if (!s) s = dmp::insph3_sos_tail(p, a, b, c, d, W);
+  return (s + 1) | (ovf ? 4 : 0);
 }
 
 __device__ __forceinline__ int side3(const Face3 &F, const float *y,
@@ -1573,9 +1616,8 @@ __device__ __forceinline__ int side3(const Face3 &F, const float *y,
   int s = dmp::orient3_rel_filter<float>(F.V[0], F.V[1], F.V[2], F.U[0], F.U[1],
                                          F.U[2], Y[0], Y[1], Y[2], 16.0f * DMP_U32);
   if (s) return s;
-  const int4 IY = fx_point<3>(F.fr, y);
-  if (F.IA.w & F.IB.w & IY.w) return dmp::orient3_fx(F.IA, F.IB, IY);
-  return dmp::orient3_slow(F.p, F.a, F.b, y, W);
+  return side3_exact(F.p[0], F.p[1], F.p[2], F.a[0], F.a[1], F.a[2], F.b[0], F.b[1], F.b[2], y[0],
+                     y[1], y[2], F.gfix, W);
 }
 
 // perturbed insph3(p, a, b, c, d) of a face query
@@ -1589,11 +1631,10 @@ __device__ __forceinline__ int insph_face3(const Face3 &F, const float *c, const
   float wq = Q[0] * Q[0] + Q[1] * Q[1] + Q[2] * Q[2];
   int s = dmp::insph3_rel_filter<float>(F.V, F.U, Z, Q, wx, wy, wz, wq, 48.0f * DMP_U32);
   if (s) return s;
-  const int4 IC = fx_point<3>(F.fr, c), ID = fx_point<3>(F.fr, d);
-  if (F.IA.w & F.IB.w & IC.w & ID.w) return dmp::insph3_fx_sos(F.IA, F.IB, IC, ID);
-  s = dmp::insph3_slow(F.p, F.a, F.b, c, d, &ovf, W);
-  if (s) return s;
-  return dmp::insph3_sos_tail(F.p, F.a, F.b, c, d, W);
+  const int r = insph_face3_exact(F.p[0], F.p[1], F.p[2], F.a[0], F.a[1], F.a[2], F.b[0], F.b[1],
+                                  F.b[2], c[0], c[1], c[2], d[0], d[1], d[2], F.gfix, W);
+  if (r & 4) ovf = 1;
+  return (r & 3) - 1;
 }
 
 #ifdef DM_C3_NOINLINE
@@ -1615,20 +1656,20 @@ __device__ __forceinline__ void consider3(const DTArgs &A, const Face3 &F, int j
   }
 }
 
+// Warp tournament: every lane ends with the winner of the lanes' bests and
+// its coordinates (bx holds each lane's best point).  Not unrolled: one
+// copy of the face predicate per call site.
 __device__ __forceinline__ int tourney3(const DTArgs &A, const Face3 &F,
-                                        int best, int &ovf,
+                                        int best, float *bx, int &ovf,
                                         dmp::ExactScratch *W) {
+#pragma unroll 1
   for (int o = 16; o; o >>= 1) {
-    int other = __shfl_xor_sync(0xffffffffu, best, o);
-    if (other >= 0 && other != best) {
-      if (best < 0) {
-        best = other;
-      } else {
-        float bx[3], ox[3];
-        load_pt<3>(A.P, best, bx);
-        load_pt<3>(A.P, other, ox);
-        if (insph_face3(F, bx, ox, ovf, W) < 0) best = other;
-      }
+    const int other = __shfl_xor_sync(0xffffffffu, best, o);
+    float ox[3];
+    for (int k = 0; k < 3; ++k) ox[k] = __shfl_xor_sync(0xffffffffu, bx[k], o);
+    if (other >= 0 && other != best && (best < 0 || insph_face3(F, bx, ox, ovf, W) < 0)) {
+      best = other;
+      for (int k = 0; k < 3; ++k) bx[k] = ox[k];
     }
   }
   return best;
@@ -1964,7 +2005,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   const double la = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
   const double lb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
   int best = -1;
-  float bx[3];
+  float bx[3] = {0.f, 0.f, 0.f};
   int cc[3];
   for (int k = 0; k < 3; ++k)
     cc[k] = cell_coord(g, (F.p[k] + F.a[k] + F.b[k]) * (1.f / 3.f), k);
@@ -1976,7 +2017,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
   // local search: the 27 cells around the face centroid
   if (lane < 27) scan_cell(cc[0] + lane % 3 - 1, cc[1] + (lane / 3) % 3 - 1, cc[2] + lane / 9 - 1);
   // after a tournament every lane holds the same winner: reload its point
-  best = tourney3(A, F, best, ovf, W);
+  best = tourney3(A, F, best, bx, ovf, W);
   if (best >= 0) load_pt<3>(A.P, best, bx);
   // no point near the face: if no hull candidate lies in H+, no point does
   // (a hull face); a candidate that does bounds the region of the search
@@ -2001,7 +2042,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
       warp_ranges(A.o_pts, s0, cnt, lane,
                   [&](float4 q) { consider3(A, F, __float_as_int(q.w), q, best, bx, ovf, W); });
     }
-    best = tourney3(A, F, best, ovf, W);
+    best = tourney3(A, F, best, bx, ovf, W);
     if (best >= 0)
       load_pt<3>(A.P, best, bx);
     else
@@ -2028,7 +2069,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
       int dx = t % 5 - 2, dy = (t / 5) % 5 - 2, dz = t / 25 - 2;
       if (max(abs(dx), max(abs(dy), abs(dz))) == 2) scan_cell(cc[0] + dx, cc[1] + dy, cc[2] + dz);
     }
-    best = tourney3(A, F, best, ovf, W);
+    best = tourney3(A, F, best, bx, ovf, W);
     rex = 2;
     if (best >= 0) load_pt<3>(A.P, best, bx);
     make_region3(R, F.p, a, b, n, nn, la, lb, best >= 0 ? bx : nullptr);
@@ -2084,7 +2125,7 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
     scan_blocks3(A, g, R, blo, bhi, cc, rex, lane,
                  [&](int j, float4 q) { consider3(A, F, j, q, best, bx, ovf, W); });
   }
-  best = tourney3(A, F, best, ovf, W);
+  best = tourney3(A, F, best, bx, ovf, W);
 #ifdef DM_L2_STATS
   // per-face trace of the watched vertex: dbg[1999] counts faces, record
   // i at dbg[2000 + 16 i]
@@ -2107,8 +2148,10 @@ __device__ __forceinline__ int gq3(const DTArgs &A, const GridParams &g, int ip,
       t[10] = __float_as_int((float)R.r2);
       t[11] = __float_as_int((float)R.R2);
       t[12] = rex;
-      t[13] = F.IA.w | (F.IB.w << 1) | ((int)F.fr.ok << 2);
-      t[14] = F.fr.g;
+      FaceFx X;
+      face_fx(X, F.p, F.a, F.b, F.gfix);
+      t[13] = X.IA.w | (X.IB.w << 1) | ((int)X.fr.ok << 2);
+      t[14] = X.fr.g;
     }
   }
 #endif
