@@ -55,7 +55,7 @@ constexpr int kNoFix = -100000;
 // level-3 star storage: per-warp slots in the workspace
 constexpr int L3_CAP_TRI = 16384, L3_CAP_OPEN = 8192, L3_WARPS = 4, L3_BLOCKS = 38;
 constexpr int kCntL3 = 11;  // counters slot: stars deferred to level 3
-constexpr int kCntL2Next = 12;  // counters slot: next escalated star for level 2 (3D)
+constexpr int kCntL2Next = 12;  // counters slot: next escalated star for level 2
 
 struct DTArgs {
   int dim;
@@ -2240,6 +2240,119 @@ __device__ __forceinline__ int tourney2(const DTArgs &A, const Edge2 &E,
   return best;
 }
 
+// Search region of a 2D edge query: the circle (c, r2) bounding every point
+// that may beat the current winner, or (full) the positive half-plane of the
+// edge p -> p + X with normal n when there is no winner yet.
+struct Region2 {
+  bool full;
+  float c[2], r2;
+  float p[2], n[2], nrm;
+};
+
+// May the box [lo, hi] hold a point of the region?  The tolerances are those
+// of the per-cell and per-block tests of the queries.
+__device__ __forceinline__ bool region_hits2(const Region2 &R, const GridParams &g,
+                                             const float *lo, const float *hi) {
+  if (!R.full) {
+    float dd = 0.f;
+    for (int k = 0; k < 2; ++k) {
+      const float e = R.c[k] < lo[k] ? lo[k] - R.c[k] : (R.c[k] > hi[k] ? R.c[k] - hi[k] : 0.f);
+      dd += e * e;
+    }
+    return dd <= R.r2 * 1.0001f + 1e-6f * g.cs * g.cs;
+  }
+  float mx = -FLT_MAX, scale = 0.f;
+  for (int corner = 0; corner < 4; ++corner) {
+    const float v0 = ((corner & 1) ? hi[0] : lo[0]) - R.p[0];
+    const float v1 = ((corner >> 1) & 1 ? hi[1] : lo[1]) - R.p[1];
+    mx = fmaxf(mx, v0 * R.n[0] + v1 * R.n[1]);
+    scale = fmaxf(scale, fmaxf(fabsf(v0), fabsf(v1)));
+  }
+  return !(mx < -1e-4f * R.nrm * scale);
+}
+
+// The points of up to four coarse blocks (b0..b3, < 0: none) that may lie in
+// the region, visited by the whole warp: lane l holds cell row l % 8 (the 8
+// cells along x at one y) of block b(l / 8).  Points of the 3x3 cells
+// around cc (already scanned) are skipped.
+constexpr int kBs2 = 8;  // coarse block edge in 2D (GridParams::bs)
+template <typename F>
+__device__ __forceinline__ void scan_block_quad2(const DTArgs &A, const GridParams &g,
+                                                 const Region2 &R, int b0, int b1, int b2, int b3,
+                                                 const int *cc, int lane, F f) {
+  const int slot = lane >> 3, r = lane & 7;
+  const int b = slot == 0 ? b0 : slot == 1 ? b1 : slot == 2 ? b2 : b3;
+  int off = 0, len = 0;
+  if (b >= 0) {
+    const int bxi = b % g.bdims[0], byi = b / g.bdims[0];
+    const int y = byi * kBs2 + r, x0 = bxi * kBs2, x1 = min(x0 + kBs2, g.dims[0]);
+    if (y < g.dims[1]) {
+      float lo[2], hi[2];
+      const int c0[2] = {x0, y}, c1[2] = {x1, y + 1};
+      for (int k = 0; k < 2; ++k) {
+        const float pad = (fabsf(g.lo[k]) + (float)g.dims[k] * g.cs) * 1e-6f;
+        lo[k] = g.lo[k] + (float)c0[k] * g.cs - pad;
+        hi[k] = g.lo[k] + (float)c1[k] * g.cs + pad;
+      }
+      if (region_hits2(R, g, lo, hi)) {
+        const int cs0 = x0 + g.dims[0] * y;
+        off = A.cell_start[cs0];
+        len = A.cell_start[cs0 + (x1 - x0)] - off;
+      }
+    }
+  }
+  warp_ranges(A.spts, off, len, lane, [&](float4 q) {
+    const int j = __float_as_int(q.w);
+    if (j < 0) return;  // duplicate
+    if (in_local(cc, cell_coord(g, q.x, 0), cell_coord(g, q.y, 1), 0, 2)) return;
+    f(j, q);
+  });
+}
+
+// Every point of the coarse blocks [blo, bhi] whose tight box meets the
+// region: lanes test 32 blocks at a time and the hits are scanned four by
+// four by the whole warp.
+template <typename F>
+__device__ __forceinline__ void scan_blocks2(const DTArgs &A, const GridParams &g,
+                                             const Region2 &R, const int *blo, const int *bhi,
+                                             const int *cc, int lane, F f) {
+  const int sx = bhi[0] - blo[0] + 1, sy = bhi[1] - blo[1] + 1;
+  if (sx <= 0 || sy <= 0) return;
+  const int64_t nb = (int64_t)sx * sy;
+  int q0 = -1, q1 = -1, q2 = -1, nq = 0;  // queued hits (warp-uniform)
+  for (int64_t t0 = 0; t0 < nb; t0 += 32) {
+    const int64_t t = t0 + lane;
+    int bid = -1;
+    if (t < nb) {
+      const int bxi = blo[0] + (int)(t % sx), byi = blo[1] + (int)(t / sx);
+      bid = bxi + g.bdims[0] * byi;
+      if (A.blk_cnt[bid] == 0) {
+        bid = -1;
+      } else {
+        const float lo[2] = {A.blk_box[6 * bid], A.blk_box[6 * bid + 1]};
+        const float hi[2] = {A.blk_box[6 * bid + 3], A.blk_box[6 * bid + 4]};
+        if (!region_hits2(R, g, lo, hi)) bid = -1;
+      }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, bid >= 0);
+    while (m) {
+      const int h = __shfl_sync(0xffffffffu, bid, __ffs(m) - 1);
+      m &= m - 1;
+      if (nq == 3) {
+        scan_block_quad2(A, g, R, q0, q1, q2, h, cc, lane, f);
+        q0 = q1 = q2 = -1;
+        nq = 0;
+      } else {
+        if (nq == 0) q0 = h;
+        else if (nq == 1) q1 = h;
+        else q2 = h;
+        ++nq;
+      }
+    }
+  }
+  if (nq) scan_block_quad2(A, g, R, q0, q1, q2, -1, cc, lane, f);
+}
+
 __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
                                    int ix, int sgn, int lane, int &ovf,
                                    dmp::ExactScratch *W) {
@@ -2326,48 +2439,27 @@ __device__ __forceinline__ int gq2(const DTArgs &A, const GridParams &g, int ip,
         for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
       }
     } else {
-      int blo[2] = {lo[0] / g.bs, lo[1] / g.bs}, bhi[2] = {hi[0] / g.bs, hi[1] / g.bs};
-      int sx = bhi[0] - blo[0] + 1;
-      int64_t nb = (int64_t)sx * (bhi[1] - blo[1] + 1);
-      for (int64_t t = lane; t < nb; t += 32) {
-        int bxi = blo[0] + (int)(t % sx), byi = blo[1] + (int)(t / sx);
-        int bid = bxi + g.bdims[0] * byi;
-        if (A.blk_cnt[bid] == 0) continue;
-        float dd = 0.f;
-        for (int k = 0; k < 2; ++k) {
-          float b0 = A.blk_box[6 * bid + k], b1 = A.blk_box[6 * bid + 3 + k];
-          float c = (float)cen[k];
-          float e = c < b0 ? b0 - c : (c > b1 ? c - b1 : 0.f);
-          dd += e * e;
-        }
-        if (dd > r2 * 1.0001f + 1e-6f * g.cs * g.cs) continue;
-        for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
-          for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
-            if (in_local(cc, x, y, 0, 2)) continue;
-            for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
-          }
-      }
+      Region2 R;
+      R.full = false;
+      R.c[0] = (float)cen[0];
+      R.c[1] = (float)cen[1];
+      R.r2 = r2;
+      const int blo[2] = {lo[0] / kBs2, lo[1] / kBs2}, bhi[2] = {hi[0] / kBs2, hi[1] / kBs2};
+      scan_blocks2(A, g, R, blo, bhi, cc, lane,
+                   [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
     }
   } else {
-    float nrm = sqrtf(E.X[0] * E.X[0] + E.X[1] * E.X[1]);
-    float n0 = -E.X[1] * sgn, n1 = E.X[0] * sgn;
-    for (int bid = lane; bid < g.nblocks; bid += 32) {
-      if (A.blk_cnt[bid] == 0) continue;
-      float mx = -FLT_MAX, scale = 0.f;
-      for (int corner = 0; corner < 4; ++corner) {
-        float v0 = A.blk_box[6 * bid + (corner & 1) * 3 + 0] - E.p[0];
-        float v1 = A.blk_box[6 * bid + ((corner >> 1) & 1) * 3 + 1] - E.p[1];
-        mx = fmaxf(mx, v0 * n0 + v1 * n1);
-        scale = fmaxf(scale, fmaxf(fabsf(v0), fabsf(v1)));
-      }
-      if (mx < -1e-4f * nrm * scale) continue;
-      int bxi = bid % g.bdims[0], byi = bid / g.bdims[0];
-      for (int y = byi * g.bs; y < min(byi * g.bs + g.bs, g.dims[1]); ++y)
-        for (int x = bxi * g.bs; x < min(bxi * g.bs + g.bs, g.dims[0]); ++x) {
-          if (in_local(cc, x, y, 0, 2)) continue;
-          for_cell(A, x + g.dims[0] * y, [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
-        }
-    }
+    // every block that may hold a point on the positive side
+    Region2 R;
+    R.full = true;
+    R.p[0] = E.p[0];
+    R.p[1] = E.p[1];
+    R.n[0] = -E.X[1] * sgn;
+    R.n[1] = E.X[0] * sgn;
+    R.nrm = sqrtf(E.X[0] * E.X[0] + E.X[1] * E.X[1]);
+    const int blo[2] = {0, 0}, bhi[2] = {g.bdims[0] - 1, g.bdims[1] - 1};
+    scan_blocks2(A, g, R, blo, bhi, cc, lane,
+                 [&](int j, float4 q) { consider2(A, E, j, q, best, bx, ovf, W); });
   }
   return tourney2(A, E, best, ovf, W);
 }
@@ -2984,8 +3076,12 @@ __global__ void __launch_bounds__(32 * L2_WARPS) k_star2_l2(DTArgs A) {
   auto &Q1 = sm1[w];
   const GridParams g = *A.gp;
   const int64_t nesc = A.counters[DM_CNT_ESCALATED];
-  for (int64_t k = (int64_t)blockIdx.x * L2_WARPS + w; k < nesc;
-       k += (int64_t)gridDim.x * L2_WARPS) {
+  // stars are taken one at a time from a shared counter, as in 3D
+  for (;;) {
+    unsigned long long kk = 0;
+    if (lane == 0) kk = atomicAdd((unsigned long long *)&A.counters[kCntL2Next], 1ull);
+    const int64_t k = (int64_t)__shfl_sync(0xffffffffu, kk, 0);
+    if (k >= nesc) break;
     int ovf = 0, ip, a, b;
     if (!seed_of2(A, g, k, Q1, lane, ovf, W, ip, a, b)) {
       if (lane == 0) flag_or(A.counters, DM_FLAG_SEED_FAILED);
