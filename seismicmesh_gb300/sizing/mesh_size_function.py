@@ -2,13 +2,18 @@
 
 Drop-in for sizing/mesh_size_function.py of the reference:
 get_sizing_function_from_segy (34-239) with the same keyword options and
-defaults, read_velocity_model (590-606) and its binary / SEG-Y readers.
+defaults, read_velocity_model (590-606) and its binary / SEG-Y readers, and
+write_velocity_model (242-335).  read_velocity_model_to_device streams a raw
+binary model from disk into a device grid; get_sizing_function_from_segy
+takes that path for binary files and accepts device tensors as
+velocity_data.
 The size grid is computed by dm_size_from_velocity (wavelength sizing,
 clamp, Courant bound), dm_limgrad (gradation limiting) and dm_pad_grid
 (domain pad); the resulting SizeFunction evaluates with dm_sizing_eval
 (linear, extrapolating interpolation like RegularGridInterpolator with
 bounds_error=False, fill_value=None).
 """
+import os
 import warnings
 
 import numpy as np
@@ -23,6 +28,7 @@ __all__ = [
     "write_velocity_model",
     "plot_sizing_function",
     "read_velocity_model",
+    "read_velocity_model_to_device",
     "GridSizing",
 ]
 
@@ -111,8 +117,10 @@ def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
     sz_opts.update(kwargs)
     vp = sz_opts["velocity_data"]
     nz, nx, ny = sz_opts["nz"], sz_opts["nx"], sz_opts["ny"]
+    owned = False  # vp is a device grid this call made (no defensive copy)
     if vp is None:
-        vp, nz, nx, ny = read_velocity_model(
+        reader = read_velocity_model if filename.endswith(".segy") else read_velocity_model_to_device
+        vp, nz, nx, ny = reader(
             filename,
             nz=nz,
             nx=nx,
@@ -122,6 +130,7 @@ def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
             axes_order_sort=sz_opts["axes_order_sort"],
             dtype=sz_opts["dtype"],
         )
+        owned = isinstance(vp, torch.Tensor)
     scale = 1.0
     if sz_opts["units"] == "km-s":
         print("Converting from km-s to m-s...", flush=True)
@@ -146,9 +155,15 @@ def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
         if key not in allowed:
             raise ValueError("Option %s with parameter %s not recognized " % (key, kwargs[key]))
 
-    vp_host = np.ascontiguousarray(np.asarray(vp, dtype=np.float64))
-    shape = vp_host.shape
-    vpd = torch.from_numpy(vp_host).to(D.device())
+    if isinstance(vp, torch.Tensor):
+        # a grid already in memory, on the device or not: used as FP64 on
+        # the device (copied unless this call read it)
+        vp_host = None
+        vpd = vp.detach().to(device=D.device(), dtype=torch.float64, copy=not owned).contiguous()
+    else:
+        vp_host = np.ascontiguousarray(np.asarray(vp, dtype=np.float64))
+        vpd = torch.from_numpy(vp_host).to(D.device())
+    shape = tuple(vpd.shape)
     cell = torch.empty_like(vpd)
     if sz_opts["wl"] < 0:
         raise ValueError("Parameter `wl` must be set > 0")
@@ -170,7 +185,10 @@ def get_sizing_function_from_segy(filename, bbox, comm=None, **kwargs):
         window = [int(st)] * dim if np.isscalar(st) else [int(w) for w in st]
         # water replacement as the reference decides it (any vp < 1e-3 in a
         # row other than the first, sizing/mesh_size_function.py:154-165)
-        replace = bool(np.any(vp_host[1:] * scale < 1e-3))
+        if vp_host is not None:
+            replace = bool(np.any(vp_host[1:] * scale < 1e-3))
+        else:
+            replace = bool((vpd[1:] * scale < 1e-3).any().item())
         vw = float(sz_opts["vp_water"]) if sz_opts["vp_water"] is not None else 0.0
         if replace and (sz_opts["vp_water"] is None or vw < 1300 or vw > 1800):
             raise ValueError("vp_water is None or out of bounds. It should be >1300 and <1800 m/s")
@@ -306,22 +324,99 @@ def read_velocity_model(
 def _read_bin(filename, nz, nx, ny, byte_order, axes_order, axes_order_sort, dtype):
     """Binary model with endianness, axis order and F/C order
     (sizing/mesh_size_function.py:609-630)."""
+    axes, fdt = _bin_layout(nz, nx, ny, byte_order, axes_order, dtype)
+    print(f"Reading binary file: {filename}")
+    vp = np.fromfile(filename, dtype=fdt)
+    vp = vp.reshape(*axes, order=axes_order_sort)
+    vp = np.flipud(vp.transpose((*axes_order,)))
+    return vp, nz, nx, ny
+
+
+def _bin_layout(nz, nx, ny, byte_order, axes_order, dtype):
+    """stored axis lengths and file dtype of a binary model, checked as
+    _read_bin checks them"""
     if (nz is None) or (nx is None) or (ny is None):
         raise ValueError(
             "Please specify the number of grid points in each dimension (e.g., `nz`, `nx`, `ny`)..."
         )
     axes = [nz, nx, ny]
-    ix = np.argsort(axes_order)
-    axes = [axes[o] for o in ix]
-    print(f"Reading binary file: {filename}")
+    stored = [axes[o] for o in np.argsort(axes_order)]
     if byte_order == "big":
-        vp = np.fromfile(filename, dtype=np.dtype(dtype).newbyteorder(">"))
+        fdt = np.dtype(dtype).newbyteorder(">")
     elif byte_order == "little":
-        vp = np.fromfile(filename, dtype=np.dtype(dtype).newbyteorder("<"))
+        fdt = np.dtype(dtype).newbyteorder("<")
     else:
         raise ValueError("Please specify byte_order as either: little or big.")
-    vp = vp.reshape(*axes, order=axes_order_sort)
-    vp = np.flipud(vp.transpose((*axes_order,)))
+    return stored, fdt
+
+
+def read_velocity_model_to_device(
+    filename, nz=None, nx=None, ny=None, byte_order=None, axes_order=None,
+    axes_order_sort=None, dtype=None, device=None, slab_bytes=1 << 26,
+):
+    """Stream a raw binary velocity model from disk into a device grid.
+
+    Returns (vp, nz, nx, ny) like read_velocity_model, with vp a float64
+    tensor on `device` (default: the current CUDA device) equal to the
+    array _read_bin returns: the file is reshaped in axes_order_sort order
+    to the stored axis lengths, transposed by axes_order and flipped along
+    its first axis (sizing/mesh_size_function.py:609-630).
+
+    The file is read in slabs of slab_bytes.  On a CUDA device two pinned
+    host buffers alternate: a slab is read and converted to native byte
+    order while the previous one is copied to the device on a side stream
+    and widened to FP64 there.  The reshape, transposition and flip are
+    index permutations applied on the device, so no host copy of the whole
+    model is made."""
+    axes_order = (0, 1, 2) if axes_order is None else tuple(axes_order)
+    stored, fdt = _bin_layout(nz, nx, ny, byte_order, axes_order, dtype)
+    if axes_order_sort not in ("F", "C", "A"):
+        raise ValueError("order must be one of 'C', 'F' or 'A'")
+    dev = D.device() if device is None else torch.device(device)
+    total = int(np.prod(stored))
+    size = os.path.getsize(filename)
+    if size != total * fdt.itemsize:
+        raise ValueError(
+            f"cannot reshape array of size {size // fdt.itemsize} into shape {tuple(stored)}"
+        )
+    print(f"Reading binary file: {filename}")
+    native = fdt.newbyteorder("=")
+    tdt = torch.from_numpy(np.zeros(1, dtype=native)).dtype
+    out = torch.empty(total, dtype=torch.float64, device=dev)
+    chunk = max(1, min(total, int(slab_bytes) // fdt.itemsize))
+    cuda = dev.type == "cuda"
+    host = [torch.empty(chunk, dtype=tdt, pin_memory=cuda) for _ in range(2)]
+    if cuda:
+        stage = [torch.empty(chunk, dtype=tdt, device=dev) for _ in range(2)]
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        done = [None, None]
+    with open(filename, "rb") as fh:
+        for k, start in enumerate(range(0, total, chunk)):
+            m = min(chunk, total - start)
+            b = k % 2
+            if cuda and done[b] is not None:
+                done[b].synchronize()  # the copy out of this pinned buffer has ended
+            raw = np.fromfile(fh, dtype=fdt, count=m)
+            if raw.size != m:
+                raise ValueError(f"{filename}: file ended after {start + raw.size} values")
+            host[b].numpy()[:m] = raw
+            if cuda:
+                with torch.cuda.stream(side):
+                    stage[b][:m].copy_(host[b][:m], non_blocking=True)
+                    out[start:start + m].copy_(stage[b][:m])
+                    done[b] = torch.cuda.Event()
+                    done[b].record(side)
+            else:
+                out[start:start + m].copy_(host[b][:m])
+    if cuda:
+        torch.cuda.current_stream(dev).wait_stream(side)
+    if axes_order_sort == "F":
+        # column-major: the C-order view of the reversed lengths, axes reversed
+        vp = out.view(*stored[::-1]).permute(2, 1, 0)
+    else:
+        vp = out.view(*stored)
+    vp = vp.permute(*axes_order).flip(0).contiguous()
     return vp, nz, nx, ny
 
 
@@ -360,13 +455,50 @@ def _read_segy(filename):
     return np.flipud(vp), ns, nx, 0
 
 
-def write_velocity_model(*args, **kwargs):
-    """HDF5 writer of the reference (242-335); needs h5py, absent here."""
+def write_velocity_model(filename, ofname=None, comm=None, **kwargs):
+    r"""Read a velocity model and write it as an HDF5 file
+    (sizing/mesh_size_function.py:242-335).
+
+    The model is read as read_velocity_model reads it (nz, nx, ny,
+    byte_order, axes_order, axes_order_sort and dtype as there), padded when
+    domain_pad > 0 (with bbox and pad_style, as the sizing call pads), and
+    written to ofname + ".hdf5" (filename + ".hdf5" without ofname, with a
+    warning) as the float32 dataset "velocity_model" with the attributes
+    shape and units = "m/s".  With a communicator only rank 0 writes.
+    Needs h5py."""
     try:
-        import h5py  # noqa: F401
+        import h5py
     except ImportError as e:
         raise ImportError("write_velocity_model needs h5py") from e
-    raise NotImplementedError("write_velocity_model is outside the GPU engine")
+    opts = {
+        "hmin": 150.0, "hmax": 10000.0, "wl": 0, "freq": 2.0, "grad": 0.0, "grade": 0.0,
+        "stencil_size": 10.0, "space_order": 1, "dt": 0.0, "cr_max": 1.0, "pad_style": "edge",
+        "domain_pad": 0.0, "units": "m-s", "nz": None, "nx": None, "ny": None,
+        "byte_order": "byte_order", "axes_order": (0, 1, 2), "axes_order_sort": "F",
+        "dtype": "float32",
+    }
+    opts.update(kwargs)
+    if comm is not None and getattr(comm, "rank", 0) != 0:
+        return
+    if ofname is None:
+        warnings.warn("No output filename specified, name will be `filename`")
+        ofname = filename
+    vp, nz, nx, ny = read_velocity_model(
+        filename, nz=opts["nz"], nx=opts["nx"], ny=opts["ny"], byte_order=opts["byte_order"],
+        axes_order=opts["axes_order"], axes_order_sort=opts["axes_order_sort"],
+        dtype=opts["dtype"],
+    )
+    if opts["domain_pad"] > 0.0:
+        print("Adding a domain pad to the velocity model...")
+        vpd = torch.from_numpy(np.ascontiguousarray(vp, dtype=np.float64)).to(D.device())
+        _, vpd, _ = _build_domain_pad(vpd, vpd, opts["bbox"], opts)
+        vp = vpd.cpu().numpy()
+    ofname += ".hdf5"
+    print(f"Writing velocity model: {ofname}", flush=True)
+    with h5py.File(ofname, "w") as f:
+        f.create_dataset("velocity_model", data=vp, dtype="f")
+        f.attrs["shape"] = vp.shape
+        f.attrs["units"] = "m/s"
 
 
 def plot_sizing_function(*args, **kwargs):

@@ -129,3 +129,30 @@ def test_3dmesher_domain_extension(cuda, style):
     p, t = sm.sliver_removal(points=p, domain=cube, edge_length=ef, h0=150, verbose=0)
     r = REFT["domain_extension_3d"][style]
     assert _close([len(p), len(t)], r["harness"]), (style, len(p), len(t), r)
+
+
+def test_sizing_from_binary_file_streams_to_the_device(cuda, tmp_path):
+    """a binary model given by file name is streamed into the device grid
+    (read_velocity_model_to_device); the size function equals, bit for bit,
+    the ones built from the same model passed as a host array and as a
+    device tensor"""
+    import torch
+
+    from seismicmesh_gb300.sizing.mesh_size_function import _read_bin
+
+    vp = golden("velocity_fixtures.npz")["bin_vp"]
+    f = tmp_path / "bin_vp.bin"
+    np.asarray(vp, dtype=np.float32).reshape(-1, order="F").astype("<f4").tofile(str(f))
+    host, *_ = _read_bin(str(f), 20, 10, 10, "little", (0, 1, 2), "F", "float32")
+    bbox = (-2e3, 0.0, 0.0, 1e3, 0.0, 1e3)
+    kw = dict(grade=0.005, nz=20, nx=10, ny=10, grad=50, freq=2, wl=10, hmin=50, domain_pad=0.0)
+    ef_file = sm.get_sizing_function_from_segy(str(f), bbox, byte_order="little", **kw)
+    ef_host = sm.get_sizing_function_from_segy(None, bbox, velocity_data=host.copy(), **kw)
+    dev = torch.from_numpy(np.ascontiguousarray(host)).cuda()
+    ef_dev = sm.get_sizing_function_from_segy(None, bbox, velocity_data=dev, **kw)
+    assert torch.equal(dev, torch.from_numpy(np.ascontiguousarray(host)).cuda())  # input untouched
+    rng = np.random.default_rng(8)
+    x = rng.uniform([-2e3, 0.0, 0.0], [0.0, 1e3, 1e3], size=(5000, 3))
+    want = ef_host.eval(x)
+    np.testing.assert_array_equal(ef_file.eval(x), want)
+    np.testing.assert_array_equal(ef_dev.eval(x), want)
