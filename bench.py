@@ -17,8 +17,10 @@ Workload: 3D unit ball (Ball((0,0,0), 1)), constant edge length h = 0.02,
           generate_mesh; time_to_mesh_s includes sliver_removal.
 
 --impl reference times the reference's CPU loop (the oracle's float64 numpy
-restatement with Qhull connectivity; CGAL and MPI are not available) on the
-same workload: the h = 0.02 ball, one DistMesh iteration per step.
+restatement; CGAL and MPI are not available, so the triangulation is the
+faster of the two stubs: the oracle's exact-predicate C++ Delaunay
+(oracle/cdt3.cpp) when it builds, else Qhull) on the same workload: the
+h = 0.02 ball, one DistMesh iteration per step.
 With torchrun (N > 1) every rank meshes its own replica; value is the sum
 over ranks (timed with a barrier and the max over ranks).
 """
@@ -169,26 +171,40 @@ def host_info():
     return {"nproc": os.cpu_count(), "cpu_model": model}
 
 
+def cpu_triangulator():
+    """the faster triangulation stub of the oracle's loop: the C++
+    exact-predicate Delaunay (3.4x Qhull on the h = 0.02 ball's iterations,
+    1.2x on its initial lattice) when it builds here, else Qhull; returns
+    (function, description)"""
+    from oracle import cdt
+
+    if cdt.available():
+        return cdt.delaunay, "the oracle's exact-predicate C++ Delaunay (oracle/cdt3.cpp)"
+    return None, "Qhull (the C++ triangulator did not build here)"
+
+
 def cpu_sample(steps, warmup, h=H):
-    """the oracle's restatement of the reference loop (float64 numpy, Qhull
-    connectivity) on the unit ball at edge length h: `warmup` untimed
-    iterations from the initial lattice, then `steps` timed ones; returns
-    (points, seconds, per-step seconds)"""
+    """the oracle's restatement of the reference loop (float64 numpy, with
+    the faster triangulation stub) on the unit ball at edge length h:
+    `warmup` untimed iterations from the initial lattice, then `steps` timed
+    ones; returns (points, seconds, per-step seconds, triangulator)"""
     from oracle import distmesh_np as O
     from oracle import sdf_np as S
+
+    tri, tri_name = cpu_triangulator()
 
     fd = S.ball(0.0, 0.0, 0.0, 1.0)
     fh = lambda x: np.full(len(x), h)  # noqa: E731
     bbox = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
     p = O.initial_points(fd, fh, h, bbox, 0.1 * h, 3)
     for _ in range(warmup):
-        p, _, _ = O.one_iteration(p, fd, fh, h)
+        p, _, _ = O.one_iteration(p, fd, fh, h, tri=tri)
     per = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        p, _, _ = O.one_iteration(p, fd, fh, h)
+        p, _, _ = O.one_iteration(p, fd, fh, h, tri=tri)
         per.append(time.perf_counter() - t0)
-    return len(p), sum(per), per
+    return len(p), sum(per), per, tri_name
 
 
 def run_reference(args, world, rank):
@@ -197,11 +213,11 @@ def run_reference(args, world, rank):
     iterations from the initial lattice, then K timed.  The reference package
     itself cannot be installed on this machine (CGAL, Boost, GMP/MPFR and
     mpi4py are absent), so its loop runs as the oracle's float64 numpy
-    restatement with Qhull connectivity; serial, as the reference's serial
-    mode is (its MPI mode is not runnable here)."""
+    restatement with the faster triangulation stub in CGAL's place; serial,
+    as the reference's serial mode is (its MPI mode is not runnable here)."""
     if rank != 0:
         return
-    n, dt, per = cpu_sample(args.steps, args.warmup)
+    n, dt, per, tri_name = cpu_sample(args.steps, args.warmup)
     value = n * args.steps / dt
     info = host_info()
     line = {
@@ -230,7 +246,7 @@ def run_reference(args, world, rank):
             "value": value, "unit": "point-iterations/s", "cores": 1, "kind": "port",
             "sample": f"{args.steps} DistMesh iterations of the h=0.02 unit ball ({n} points) after "
                       f"{args.warmup} warm-up iterations: float64 numpy restatement of the reference "
-                      "loop with Qhull connectivity (CGAL not installable), serial; "
+                      f"loop, triangulated by {tri_name} (CGAL not installable), serial; "
                       f"host {info['nproc']} cores, {info['cpu_model']}",
         },
         "e2e": {"value": value, "unit": "point-iterations/s", "h2d_bytes_per_step": 0,
@@ -417,13 +433,13 @@ def run_ours(args, world, rank, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        ncpu, dt, _ = cpu_sample(1, 0)
+        ncpu, dt, _, tri_name = cpu_sample(1, 0)
         info = host_info()
         cpu = {
             "value": ncpu / dt, "unit": "point-iterations/s", "cores": 1, "kind": "port",
             "sample": f"1 DistMesh iteration of the h=0.02 unit ball ({ncpu} points) from the initial "
-                      "lattice: float64 numpy restatement of the reference loop with Qhull "
-                      f"connectivity, serial; host {info['nproc']} cores, {info['cpu_model']}",
+                      "lattice: float64 numpy restatement of the reference loop, triangulated by "
+                      f"{tri_name}, serial; host {info['nproc']} cores, {info['cpu_model']}",
         }
     if rank == 0:
         line = {

@@ -1,11 +1,13 @@
-"""Builds the oracle's C restatement (test infrastructure) into oracle/lib/,
-and the reference's own C++ modules into oracle/_ref/ when the reference
-sources and pybind11 are available."""
+"""Builds the oracle's C restatement and its C++ triangulator (test
+infrastructure) into oracle/lib/, and the reference's own C++ modules into
+oracle/_ref/ when the reference sources and pybind11 are available."""
 import os
 import subprocess
+import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "lib", "liboracle.so")
+CDT = os.path.join(HERE, "lib", "libcdt3.so")
 
 
 def build_oracle_c():
@@ -15,6 +17,24 @@ def build_oracle_c():
         return LIB
     subprocess.run(["gcc", "-O2", "-shared", "-fPIC", "-ffp-contract=off", src, "-o", LIB, "-lm"], check=True)
     return LIB
+
+
+def build_cdt():
+    """the exact-predicate C++ triangulator (oracle/cdt3.cpp); returns None,
+    after a note on stderr, when no C++ compiler builds it"""
+    src = os.path.join(HERE, "cdt3.cpp")
+    if os.path.exists(CDT) and os.path.getmtime(CDT) > os.path.getmtime(src):
+        return CDT
+    os.makedirs(os.path.dirname(CDT), exist_ok=True)
+    cmd = ["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off", src, "-o", CDT + ".tmp"]
+    try:
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+        os.replace(CDT + ".tmp", CDT)
+    except (OSError, subprocess.CalledProcessError) as e:
+        err = getattr(e, "stderr", "") or str(e)
+        print("oracle: the C++ triangulator was not built: " + err.strip()[:500], file=sys.stderr)
+        return None
+    return CDT
 
 
 def reference_dir():
@@ -38,6 +58,7 @@ def build_ref():
 
 def build_all():
     build_oracle_c()
+    build_cdt()
     build_ref()
 
 

@@ -105,14 +105,16 @@ def project_back(p, fd, deps, hmin, level):
     return p
 
 
-def one_iteration(p, fd, fh, h0, levels=None, nfix=0, delta_t=0.30, geps_mult=0.1):
+def one_iteration(p, fd, fh, h0, levels=None, nfix=0, delta_t=0.30, geps_mult=0.1, tri=None):
     """triangulate, filter, forces, update, project: the body of the
-    generate_mesh loop (mesh_generator.py:460-527) for a fixed point order"""
+    generate_mesh loop (mesh_generator.py:460-527) for a fixed point order;
+    tri: the triangulation stub (default Qhull; oracle.cdt.delaunay is the
+    exact-predicate C++ one)"""
     dim = p.shape[1]
     L0mult = 1 + 0.4 / 2 ** (dim - 1)
     geps = geps_mult * h0
     deps = np.sqrt(EPS) * h0
-    t = remove_outside(p, delaunay(p), fd, geps)
+    t = remove_outside(p, (tri or delaunay)(p), fd, geps)
     F = bar_forces(p, t, fh, L0mult)
     F[:nfix] = 0
     p = p + delta_t * F
