@@ -177,10 +177,25 @@ def cpu_triangulator():
     1.2x on its initial lattice) when it builds here, else Qhull; returns
     (function, description)"""
     from oracle import cdt
+    from oracle import distmesh_np as O
 
-    if cdt.available():
-        return cdt.delaunay, "the oracle's exact-predicate C++ Delaunay (oracle/cdt3.cpp)"
-    return None, "Qhull (the C++ triangulator did not build here)"
+    if not cdt.available():
+        return None, "Qhull (the C++ triangulator did not build here)"
+    fallbacks = []
+
+    def tri(p):
+        try:
+            return cdt.delaunay(p)
+        except RuntimeError as e:  # reported in the line, never expected
+            fallbacks.append(str(e))
+            return O.delaunay(p)
+
+    class Name:
+        def __str__(self):
+            extra = f"; Qhull on {len(fallbacks)} iterations it failed" if fallbacks else ""
+            return "the oracle's exact-predicate C++ Delaunay (oracle/cdt3.cpp)" + extra
+
+    return tri, Name()
 
 
 def cpu_sample(steps, warmup, h=H):
