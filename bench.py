@@ -173,8 +173,8 @@ def host_info():
 
 def cpu_triangulator():
     """the faster triangulation stub of the oracle's loop: the C++
-    exact-predicate Delaunay (3.4x Qhull on the h = 0.02 ball's iterations,
-    1.2x on its initial lattice) when it builds here, else Qhull; returns
+    exact-predicate Delaunay (1.7-3x Qhull on the h = 0.02 ball's iterations,
+    2.7x on its initial lattice) when it builds here, else Qhull; returns
     (function, description)"""
     from oracle import cdt
     from oracle import distmesh_np as O

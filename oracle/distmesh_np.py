@@ -53,12 +53,23 @@ def delaunay(p):
 
 def unique_edges(t):
     """_get_edges + unique_edges (mesh_generator.py:680-688,
-    fast_geometry.cpp:30-77): sorted unique (min, max) pairs."""
+    fast_geometry.cpp:30-77): sorted unique (min, max) pairs.  Each pair is
+    one int64 key min * n + max, whose order is the lexicographic order of
+    the pairs, so one integer sort does what the reference's std::sort of
+    pairs does (a row-wise np.unique took ten times the reference's time).
+    Sorting, then dropping repeats, is one tenth of np.unique's time on the
+    18.7 M keys of the h = 0.02 ball."""
     dim = t.shape[1] - 1
     pairs = [(0, 1), (1, 2), (2, 0)] + ([(0, 3), (1, 3), (2, 3)] if dim == 3 else [])
-    e = np.concatenate([t[:, list(pr)] for pr in pairs])
-    e = np.sort(e, axis=1)
-    return np.unique(e, axis=0)
+    t = np.asarray(t, dtype=np.int64)
+    if len(t) == 0:
+        return np.zeros((0, 2), dtype=np.int64)
+    n = int(t.max()) + 1
+    i = np.concatenate([t[:, a] for a, _ in pairs])
+    j = np.concatenate([t[:, b] for _, b in pairs])
+    key = np.sort(np.minimum(i, j) * n + np.maximum(i, j))
+    key = key[np.concatenate([[True], key[1:] != key[:-1]])]  # np.unique is slow here
+    return np.stack([key // n, key % n], axis=1)
 
 
 def remove_outside(p, t, fd, geps):
