@@ -24,3 +24,30 @@ def test_measured_traffic_reads_both_profiles():
 
     t = bench.measured_traffic()
     assert t is not None and t > 0
+
+
+def test_cpu_triangulator_falls_back_to_qhull_and_says_so(monkeypatch):
+    """the CPU loop's stub: the C++ triangulator when it builds; an
+    iteration on which it fails (planted here, on the CPU) is triangulated
+    by Qhull and the sample text reports it"""
+    import numpy as np
+
+    import bench
+    from oracle import cdt
+
+    if not cdt.available():
+        pytest.skip("no C++ compiler for oracle/cdt3.cpp")
+    p = np.random.default_rng(1).random((300, 3))
+    tri, name = bench.cpu_triangulator()
+    assert "C++" in str(name) and "Qhull" not in str(name)
+    assert len(tri(p)) > 0
+
+    def broken(_):
+        raise RuntimeError("cdt3_delaunay failed (planted)")
+
+    monkeypatch.setattr(cdt, "delaunay", broken)
+    t = tri(p)
+    from scipy.spatial import Delaunay
+
+    assert np.array_equal(np.sort(t, 1), np.sort(Delaunay(p).simplices, 1))
+    assert "Qhull on 1 iterations" in str(name)
