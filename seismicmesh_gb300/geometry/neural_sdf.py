@@ -8,7 +8,7 @@ tensor cores (dm_mlp_eval: BF16 weights and activations, FP32 accumulation
 in tensor memory).  Distances are clamped to +-clamp during training, so the
 network answers "how far, up to clamp" and the sign.
 
-The exact SDF stays the judge near the boundary: wherever the network's
+The exact SDF decides near the boundary: wherever the network's
 value lies within `band` = 2 hmin + margin * (largest error measured on
 held-out samples) of the surface, and everywhere a point may lie outside
 (where DistMesh projects it), the exact distance replaces it.  Decisions
