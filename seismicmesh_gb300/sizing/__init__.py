@@ -4,6 +4,7 @@ from .mesh_size_function import (
     get_sizing_function_from_segy,
     plot_sizing_function,
     read_velocity_model,
+    read_velocity_model_to_device,
     write_velocity_model,
 )
 from .size_function import SizeFunction
@@ -14,5 +15,6 @@ __all__ = [
     "get_sizing_function_from_segy",
     "plot_sizing_function",
     "read_velocity_model",
+    "read_velocity_model_to_device",
     "write_velocity_model",
 ]
