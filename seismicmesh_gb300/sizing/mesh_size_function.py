@@ -351,8 +351,8 @@ def _bin_layout(nz, nx, ny, byte_order, axes_order, dtype):
 
 
 def read_velocity_model_to_device(
-    filename, nz=None, nx=None, ny=None, byte_order=None, axes_order=None,
-    axes_order_sort=None, dtype=None, device=None, slab_bytes=1 << 26,
+    filename, nz=None, nx=None, ny=None, byte_order=None, axes_order=(0, 1, 2),
+    axes_order_sort="F", dtype="float32", device=None, slab_bytes=1 << 26,
 ):
     """Stream a raw binary velocity model from disk into a device grid.
 
@@ -367,8 +367,12 @@ def read_velocity_model_to_device(
     order while the previous one is copied to the device on a side stream
     and widened to FP64 there.  The reshape, transposition and flip are
     index permutations applied on the device, so no host copy of the whole
-    model is made."""
+    model is made.  The defaults of axes_order, axes_order_sort and dtype
+    are those of get_sizing_function_from_segy; nz, nx, ny and byte_order
+    are required, as for _read_bin."""
     axes_order = (0, 1, 2) if axes_order is None else tuple(axes_order)
+    axes_order_sort = "F" if axes_order_sort is None else axes_order_sort
+    dtype = "float32" if dtype is None else dtype
     stored, fdt = _bin_layout(nz, nx, ny, byte_order, axes_order, dtype)
     if axes_order_sort not in ("F", "C", "A"):
         raise ValueError("order must be one of 'C', 'F' or 'A'")
