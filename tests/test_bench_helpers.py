@@ -51,3 +51,19 @@ def test_cpu_triangulator_falls_back_to_qhull_and_says_so(monkeypatch):
 
     assert np.array_equal(np.sort(t, 1), np.sort(Delaunay(p).simplices, 1))
     assert "Qhull on 1 iterations" in str(name)
+
+
+def test_batch_stream_assignment_is_largest_first_least_loaded():
+    """generate_meshes captures the problems on S streams: the largest first,
+    each to the stream with the least work so far (host logic, no GPU)"""
+    from seismicmesh_gb300.generation.batch import _assign
+
+    sizes = [5, 100, 30, 30, 70, 1]
+    a = _assign(sizes, 3)
+    assert sorted(a) == list(range(len(sizes)))
+    load = [0, 0, 0]
+    for i, s in enumerate(sizes):
+        load[a[i]] += s
+    assert sorted(load) == [66, 70, 100]  # 100 | 70 | 30 + 30 + 5 + 1
+    assert a[1] != a[4]  # the two largest go to different streams
+    assert _assign([7], 4) == {0: 0}
