@@ -384,7 +384,8 @@ struct DT {
   int last = 0;
   uint32_t rng = 12345u;
   bool broken = false;  // a cavity boundary that did not close (never expected)
-  std::vector<int> made;
+  std::vector<int> made, outf;
+  std::vector<Tet> newt;
   std::vector<uint64_t> slot_key;
   std::vector<int> slot_val;
 
@@ -468,10 +469,36 @@ struct DT {
         }
       }
     }
-    // new tetrahedra: cavity tetrahedron c with its vertex k replaced by p
+    // new tetrahedra: cavity tetrahedron c with its vertex k replaced by p.
+    // Every boundary face is read first: the cavity's slots are reused for
+    // the new cone (they were just read, so they are in cache), and the face
+    // of the outside neighbour is found by its vertices, not by the slot.
     const size_t nb = bnd_t.size();
+    newt.resize(nb);
+    outf.resize(nb);
     made.resize(nb);
-    for (size_t i = 0; i < nb; ++i) made[i] = fresh();
+    for (size_t i = 0; i < nb; ++i) {
+      const int c = bnd_t[i], k = bnd_k[i];
+      Tet T = tets[c];
+      T.v[k] = p;
+      int jj = -1;
+      const int out = T.nb[k];
+      if (out >= 0) {
+        const Tet &O = tets[out];
+        for (int j = 0; j < 4 && jj < 0; ++j) {
+          bool in_face = false;
+          for (int l = 0; l < 4; ++l) in_face = in_face || (l != k && T.v[l] == O.v[j]);
+          if (!in_face) jj = j;
+        }
+      }
+      newt[i] = T;
+      outf[i] = jj;
+    }
+    for (size_t i = 0; i < nb; ++i) made[i] = i < cav.size() ? cav[i] : fresh();
+    for (size_t r = nb; r < cav.size(); ++r) {
+      tets[cav[r]].v[0] = -1;
+      freel.push_back(cav[r]);
+    }
     // faces through p are matched by their edge (the two other vertices) in
     // an open-addressing table; each edge of the cavity boundary is met twice
     size_t cap2 = 16;
@@ -483,15 +510,10 @@ struct DT {
     for (size_t i = 0; i < cap2; ++i) slot_key[i] = ~0ull;
     size_t unmatched = 0;
     for (size_t i = 0; i < nb; ++i) {
-      const int c = bnd_t[i], k = bnd_k[i], m = made[i];
-      Tet T = tets[c];
-      T.v[k] = p;
-      const int out = tets[c].nb[k];
-      T.nb[k] = out;
-      if (out >= 0) {
-        for (int j = 0; j < 4; ++j)
-          if (tets[out].nb[j] == c) tets[out].nb[j] = m;
-      }
+      const int k = bnd_k[i], m = made[i];
+      Tet T = newt[i];
+      const int out = T.nb[k];
+      if (out >= 0) tets[out].nb[outf[i]] = m;
       for (int j = 0; j < 4; ++j) {
         if (j == k) continue;
         int e0 = -1, e1 = -1;
@@ -521,10 +543,6 @@ struct DT {
       mark[m] = 0;
     }
     if (unmatched) broken = true;
-    for (int c : cav) {
-      tets[c].v[0] = -1;
-      freel.push_back(c);
-    }
     last = made[0];
     return true;
   }
