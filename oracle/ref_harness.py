@@ -8,7 +8,9 @@ The reference imports modules that cannot be installed here:
   * matplotlib              -> empty modules (plotting only)
   * pyamg                   -> ruge_stuben_solver(A).solve(b) by a direct sparse solve
   * _delaunay_class(3)      -> CGAL triangulations; stood in for by Qhull
-                               (scipy.spatial.Delaunay), duplicates merged
+                               (scipy.spatial.Delaunay), duplicates merged;
+                               in 3D optionally by the oracle's exact-predicate
+                               C++ Delaunay (use_cpp_triangulator)
   * _delaunay, _cpputils    -> CGAL helpers off the serial hot path
   * _fast_geometry, _FastHJ -> built from the reference's own C++ sources
                                (oracle/Makefile -> oracle/_ref/)
@@ -87,9 +89,8 @@ def _install_stubs():
         def insert(self, flat):
             q = np.asarray(flat, dtype=float).reshape(-1, self.dim)
             self.p = np.vstack((self.p, q))
-            # CGAL keeps one vertex per location
-            _, idx = np.unique(self.p, axis=0, return_index=True)
-            self.p = self.p[np.sort(idx)]
+            # CGAL keeps one vertex per location (the first)
+            self.p = self.p[_first_occurrences(self.p)]
 
         def move(self, ids, flat):
             q = np.asarray(flat, dtype=float).reshape(-1, self.dim)
@@ -105,6 +106,8 @@ def _install_stubs():
             return self.p.copy()
 
         def get_finite_cells(self):
+            if self.dim == 3 and _tri3 is not None:
+                return _tri3(self.p).astype(np.int32)
             return Delaunay(self.p).simplices.astype(np.int32)
 
     class DT2(_DT):
@@ -139,6 +142,30 @@ def _install_stubs():
 
 
 _loaded = None
+_tri3 = None  # 3D triangulation stub: None for Qhull, else points -> tetrahedra
+
+
+def use_cpp_triangulator(on=True):
+    """Triangulate 3D sets with the oracle's exact-predicate C++ Delaunay
+    (oracle/cdt3.cpp) in CGAL's place instead of Qhull."""
+    global _tri3
+    if on:
+        from . import cdt
+
+        _tri3 = cdt.delaunay
+    else:
+        _tri3 = None
+
+
+def _first_occurrences(p):
+    """mask of the rows of p that equal no earlier row (what CGAL keeps)"""
+    if len(p) < 2:
+        return np.ones(len(p), dtype=bool)
+    order = np.lexsort(p.T[::-1])  # stable: equal rows keep their input order
+    s = p[order]
+    later = np.zeros(len(p), dtype=bool)
+    later[order[1:]] = np.all(s[1:] == s[:-1], axis=1)
+    return ~later
 
 
 def load():

@@ -4,14 +4,19 @@ bound), run through oracle/ref_harness.py in the build container:
 
     python tests/golden/make_golden_ball_h002.py           # about 30 min, 1 core
     python tests/golden/make_golden_ball_h002.py --jitter  # same, generic start
+    python tests/golden/make_golden_ball_h002.py --cpp     # the C++ triangulator
 
 Writes tests/golden/ball_h002.json (counts, dihedral and quality
 statistics, volume, wall times).  With --jitter the run starts from the
 same initial points moved by a seeded uniform jitter of +-1e-3 h (rounded
 to float32; oracle/distmesh_np.py jittered_ball_points), where every
 Delaunay triangulation of the run is unique, and writes
-ball_h002_jitter.json.  The GPU tests compare the package's generate_mesh +
-sliver_removal with these numbers.
+ball_h002_jitter.json.  With --cpp the 3D triangulations are the oracle's
+exact-predicate C++ Delaunay (oracle/cdt3.cpp) instead of Qhull, and the run
+writes ball_h002_cpp.json: the reference loop timed with the faster of the
+two triangulation stubs, and a second exact-triangulation run whose ties are
+broken differently from Qhull's.  The GPU tests compare the package's
+generate_mesh + sliver_removal with these numbers.
 """
 import json
 import os
@@ -47,6 +52,9 @@ def metrics(p, t):
 def main():
     h = 0.02
     jitter = "--jitter" in sys.argv
+    cpp = "--cpp" in sys.argv
+    if cpp:
+        ref_harness.use_cpp_triangulator()
     ball = SM.Ball([0.0, 0.0, 0.0], 1.0)
     kw = {"points": O.jittered_ball_points(h)} if jitter else {}
     t0 = time.perf_counter()
@@ -62,11 +70,13 @@ def main():
     out = {
         "workload": "3D unit ball, h=0.02, max_iter 50, seed 0, sliver_removal(min_dh_angle_bound=10)"
                     + (", initial points jittered by U(-1e-3 h, 1e-3 h), seed 0" if jitter else ""),
-        "engine": "reference loop (SeismicMesh generation/mesh_generator.py) with Qhull standing in for CGAL",
+        "engine": "reference loop (SeismicMesh generation/mesh_generator.py) with "
+                  + ("the oracle's exact-predicate C++ Delaunay (oracle/cdt3.cpp)" if cpp else "Qhull")
+                  + " standing in for CGAL",
         "generate_mesh": m_gen, "sliver_removal": m_sl,
         "generate_mesh_s": t1 - t0, "sliver_removal_s": t3 - t2,
     }
-    name = "ball_h002_jitter.json" if jitter else "ball_h002.json"
+    name = "ball_h002" + ("_jitter" if jitter else "") + ("_cpp" if cpp else "") + ".json"
     with open(os.path.join(HERE, name), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", name)
