@@ -175,3 +175,18 @@ def test_min_sin_dihedral_against_reference_dihedral_angles():
     _, s = Q.cell_quality(p, t[ok])
     ref = np.sin(g["dihedral"].reshape(-1, 6)[ok]).min(1) / (2 * np.sqrt(2) / 3)
     np.testing.assert_allclose(s, ref, rtol=1e-8, atol=1e-12)
+
+
+def test_kat_point_in_tetrahedron_from_the_reference_test():
+    """tests/test_ptin.py of the reference: on its perfect tetrahedron the
+    query (0.5, 0.5, 1.0) is inside and (0, 0, 1) outside; the oracle's
+    restatement of vertex_in_entity3 (used by the overlap oracle) agrees, and
+    so does the 2D one on a triangle"""
+    from oracle import mesh_qa_np as QA
+
+    tet = np.array([[0, 0, 0], [0, 1, 0], [np.sqrt(2), 0.5, 0], [0.5, 0.5, np.sqrt(2)]], dtype=float)
+    assert QA.inside3((0.5, 0.5, 1.0), tet)
+    assert not QA.inside3((0.0, 0.0, 1.0), tet)
+    tri = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0]])
+    assert QA.inside2((0.25, 0.25), tri)
+    assert not QA.inside2((1.0, 1.0), tri)
