@@ -7,7 +7,10 @@ triangulation stub of the reference loop's CPU baseline:
   up to the convex hull's, and no point lies strictly inside a circumsphere
   (checked with its exact in-sphere predicate, itself checked against
   rational arithmetic);
-* exact duplicates are left out.
+* exact duplicates are left out;
+* degenerate inputs (too few, coplanar, collinear, coincident points) give
+  no tetrahedra, and points far from the origin, where Qhull's floating
+  point fails, still give an exact tiling.
 """
 from fractions import Fraction
 
@@ -166,3 +169,36 @@ def test_oracle_iteration_with_the_cpp_stub():
     a, _, _ = O.one_iteration(p.copy(), fd, fh, h)
     b, _, _ = O.one_iteration(p.copy(), fd, fh, h, tri=cdt.delaunay)
     np.testing.assert_array_equal(a, b)
+
+
+def test_degenerate_and_far_inputs():
+    """fewer than four points, coplanar, collinear and coincident sets give
+    no tetrahedra (and no error); points a million units from the origin
+    with unit spread, where Qhull's floating point breaks down, still give an
+    exact Delaunay tiling"""
+    rng = np.random.default_rng(3)
+    for n in range(4):
+        assert len(cdt.delaunay(rng.random((n, 3)))) == 0
+    assert len(cdt.delaunay(np.c_[rng.random((50, 2)), np.zeros(50)])) == 0
+    assert len(cdt.delaunay(np.c_[np.linspace(0, 1, 20), np.zeros((20, 2))])) == 0
+    assert len(cdt.delaunay(np.zeros((10, 3)))) == 0
+    q = rng.random((600, 3))
+    p = q + 1e6
+    t = cdt.delaunay(p)
+    local = p - 1e6  # exact (Sterbenz): geometry measured without cancellation
+    tree = cKDTree(local)
+    vol = 0.0
+    for tet in t:
+        s = cdt.orient4(*p[tet])
+        assert s != 0
+        v = tet if s > 0 else tet[[1, 0, 2, 3]]
+        X = local[v]
+        vol += abs(np.linalg.det(X[1:] - X[0])) / 6
+        A = 2 * (X[1:] - X[0])
+        cen = np.linalg.solve(A, (X[1:] ** 2).sum(1) - (X[0] ** 2).sum())
+        r = np.sqrt(((X[0] - cen) ** 2).sum())
+        for j in tree.query_ball_point(cen, r * (1 + 1e-6) + 1e-12):
+            if j not in v:
+                assert cdt.insphere(*p[v], p[j]) <= 0, (v, j)  # exact, on the far points
+    hv = ConvexHull(local).volume
+    assert abs(vol - hv) <= 1e-9 * hv
